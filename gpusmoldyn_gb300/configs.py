@@ -1,0 +1,178 @@
+"""Seeded synthetic systems with the shapes of the benchmark configurations.
+
+No public dataset is involved: initial positions are drawn uniformly in the
+box from numpy's Philox generator with the configuration's seed.
+
+* c1: irreversible A + B -> C, 20k + 20k in a 10 um cube, D 1/1/0.5, k 0.01,
+  dt 1 ms (the reference-scale CPU-runnable case).
+* c2: reversible A + B <-> C, 500k + 500k in a 60 um cube, k_on 0.05,
+  k_off 10, dt 0.5 ms.
+* c3: 8-species network, 16M particles in a 200 um cube, 12 reactions
+  (2 zeroth, 4 first, 5 hetero- and 1 homodimeric second order), D log-uniform
+  0.1-10, rates log-uniform over a decade, dt 1 ms, production balancing loss.
+* c4: 256 instances of the c2 network, N log-uniform 1e3-1e6 (about 37M),
+  per-instance D and k_on scaled log-uniform over a decade, c2 density.
+* c5: serving jobs, c3 network, N log-uniform 1e3-5e6, steps U[100, 10000],
+  Poisson arrivals at 50/s.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .system import System
+
+
+def rng(seed):
+    return np.random.Generator(np.random.Philox(seed))
+
+
+def uniform_positions(g, n, lo, hi):
+    lo = np.asarray(lo, np.float32)
+    hi = np.asarray(hi, np.float32)
+    p = lo + (hi - lo) * g.random((n, 3), dtype=np.float32)
+    return np.minimum(np.maximum(p, lo), hi).astype(np.float32)
+
+
+# ---------------------------------------------------------------- c1 / c2
+def build_c1(n_a=20000, n_b=20000, side=10.0, seed=1, normals="boxmuller", **kw):
+    s = System((0, 0, 0), (side, side, side), dt=1e-3, seed=seed, normals=normals, **kw)
+    A, B, Cc = s.add_species(1.0), s.add_species(1.0), s.add_species(0.5)
+    s.add_reaction(2, [A, B], [Cc], 0.01)
+    s.finalize()
+    g = rng(seed)
+    pos = uniform_positions(g, n_a + n_b, (0, 0, 0), (side, side, side))
+    sp = np.concatenate([np.full(n_a, A), np.full(n_b, B)]).astype(np.int32)
+    s.set_particles(pos, sp)
+    return s
+
+
+def c2_network(s, kon=0.05, koff=10.0):
+    A, B, Cc = s.add_species(1.0), s.add_species(1.0), s.add_species(0.5)
+    fwd = s.add_reaction(2, [A, B], [Cc], kon)
+    back = s.add_reaction(1, [Cc], [A, B], koff)
+    s.set_product_placement(back, L.BD_PP_PGEMMAX, 0.2)
+    return A, B, Cc, fwd, back
+
+
+def build_c2(n_a=500000, n_b=500000, side=60.0, seed=2, normals="boxmuller", **kw):
+    s = System((0, 0, 0), (side, side, side), dt=5e-4, seed=seed, normals=normals, **kw)
+    A, B, Cc, _, _ = c2_network(s)
+    s.finalize()
+    g = rng(seed)
+    pos = uniform_positions(g, n_a + n_b, (0, 0, 0), (side, side, side))
+    sp = np.concatenate([np.full(n_a, A), np.full(n_b, B)]).astype(np.int32)
+    s.set_particles(pos, sp)
+    return s
+
+
+# ---------------------------------------------------------------------- c3
+def c3_network(seed=3):
+    """Species diffusion coefficients and the 12 reactions (order, reactants,
+    products, rate) of the 8-species network; zeroth-order rates are per
+    volume and set so production balances loss at the initial composition."""
+    g = rng(seed)
+    D = np.exp(g.uniform(math.log(0.1), math.log(10.0), 8)).astype(np.float32)
+    k1 = np.exp(g.uniform(math.log(1.0), math.log(10.0), 4))
+    k2 = np.exp(g.uniform(math.log(0.01), math.log(0.1), 6))
+    rx = [
+        (1, [2], [], k1[0]),          # S2 -> 0
+        (1, [3], [], k1[1]),          # S3 -> 0
+        (1, [4], [2], k1[2]),         # S4 -> S2
+        (1, [5], [3], k1[3]),         # S5 -> S3
+        (2, [0, 1], [2], k2[0]),      # S0 + S1 -> S2
+        (2, [0, 3], [4], k2[1]),      # S0 + S3 -> S4
+        (2, [1, 4], [5], k2[2]),      # S1 + S4 -> S5
+        (2, [2, 6], [7], k2[3]),      # S2 + S6 -> S7
+        (2, [5, 7], [6], k2[4]),      # S5 + S7 -> S6
+        (2, [6, 6], [7], k2[5]),      # S6 + S6 -> S7
+    ]
+    return D, rx
+
+
+def c3_zeroth_rate(D, rx, density):
+    """Production per unit volume and time that balances the loss of
+    particles at a uniform composition of `density` per species."""
+    rho = density / 8.0
+    loss = 0.0
+    for order, rc, pr, k in rx:
+        if order == 1 and not pr:
+            loss += k * rho
+        if order == 2:
+            loss += (len(rc) - len(pr)) * k * rho * rho * (0.5 if rc[0] == rc[1] else 1.0)
+    return loss / 2.0
+
+
+def build_c3(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
+    s = System((0, 0, 0), (side, side, side), dt=1e-3, seed=seed, normals=normals, **kw)
+    D, rx = c3_network(network_seed)
+    for d in D:
+        s.add_species(float(d))
+    z = c3_zeroth_rate(D, rx, n / side ** 3)
+    s.add_reaction(0, [], [0], z)
+    s.add_reaction(0, [], [1], z)
+    for order, rc, pr, k in rx:
+        s.add_reaction(order, rc, pr, float(k))
+    s.finalize()
+    g = rng(seed)
+    pos = uniform_positions(g, n, (0, 0, 0), (side, side, side))
+    sp = (np.arange(n) % 8).astype(np.int32)
+    s.set_particles(pos, sp)
+    return s
+
+
+# ---------------------------------------------------------------------- c4
+C2_DENSITY = 1_000_000 / 60.0 ** 3
+
+
+def c4_instances(n_inst=256, seed=4, n_lo=1e3, n_hi=1e6):
+    g = rng(seed)
+    counts = np.exp(g.uniform(math.log(n_lo), math.log(n_hi), n_inst)).astype(np.int64)
+    counts += counts % 2  # even: half A, half B
+    dsc = np.exp(g.uniform(math.log(10 ** -0.5), math.log(10 ** 0.5), n_inst))
+    ksc = np.exp(g.uniform(math.log(10 ** -0.5), math.log(10 ** 0.5), n_inst))
+    inst = []
+    for k in range(n_inst):
+        side = float((counts[k] / C2_DENSITY) ** (1.0 / 3.0))
+        inst.append(dict(box_lo=(0.0, 0.0, 0.0), box_hi=(side, side, side), seed=1000 + k,
+                         d_scale=float(dsc[k]), k2_scale=float(ksc[k])))
+    return inst, counts
+
+
+def c4_positions(inst, counts, seed=4):
+    g = rng(seed + 1)
+    pos, sp = [], []
+    for d, n in zip(inst, counts):
+        pos.append(uniform_positions(g, int(n), d["box_lo"], d["box_hi"]))
+        sp.append(np.concatenate([np.zeros(n // 2, np.int32), np.ones(n - n // 2, np.int32)]))
+    return np.concatenate(pos), np.concatenate(sp)
+
+
+def build_c4(n_inst=256, seed=4, normals="boxmuller", n_lo=1e3, n_hi=1e6, **kw):
+    inst, counts = c4_instances(n_inst, seed, n_lo, n_hi)
+    s = System(dt=5e-4, seed=seed, normals=normals, instances=inst, **kw)
+    c2_network(s)
+    s.finalize()
+    pos, sp = c4_positions(inst, counts, seed)
+    s.set_ensemble_particles(pos, sp, counts)
+    return s, inst, counts
+
+
+def build_c2_instance(d, n, seed=4, normals="boxmuller", **kw):
+    """One c4 instance alone, as a single system with the same parameters."""
+    s = System(dt=5e-4, seed=seed, normals=normals, instances=[d], **kw)
+    c2_network(s)
+    s.finalize()
+    return s
+
+
+# ---------------------------------------------------------------------- c5
+def c5_jobs(n_jobs, seed=5, rate_hz=50.0, n_lo=1e3, n_hi=5e6, steps_lo=100, steps_hi=10000):
+    g = rng(seed)
+    arrivals = np.cumsum(g.exponential(1.0 / rate_hz, n_jobs))
+    ns = np.exp(g.uniform(math.log(n_lo), math.log(n_hi), n_jobs)).astype(np.int64)
+    steps = g.integers(steps_lo, steps_hi + 1, n_jobs)
+    return [dict(id=k, arrival=float(arrivals[k]), n=int(ns[k]), steps=int(steps[k]), seed=5000 + k)
+            for k in range(n_jobs)]

@@ -1,0 +1,1036 @@
+// bd_api.cpp -- implementation of the C ABI declared in include/gpusmoldyn.h.
+//
+// The handle owns the reaction network, the derived parameter blocks, every
+// device buffer and a CUDA graph of one (and of kGraphBatch) timesteps.  A
+// step never synchronises with the host: counts, capacity checks and the
+// step counter live in a device control block, so bd_step only launches
+// graphs.  bd_synchronize is where the host looks at the control block,
+// grows buffers after an overflow and replays the steps that did not commit
+// (a step that overflows writes only into buffers that the next attempt
+// overwrites, so replay is exact).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/gpusmoldyn.h"
+#include "bd_kernels.h"
+#include "bd_layout.h"
+#include "bd_params.h"
+
+using namespace bd;
+
+namespace {
+
+constexpr int kGraphBatch = 16;
+
+thread_local std::string g_last_error;
+
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+#define BD_CUDA(call)                                   \
+  do {                                                  \
+    if (!cuda_ok((call), #call)) return BD_ERR_CUDA;    \
+  } while (0)
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+struct bd_system {
+  bd_config cfg{};
+  std::vector<bd_instance_desc> idesc;
+  std::vector<float> D;
+  std::vector<ReactionDef> rx;
+  bool finalized = false;
+  std::vector<DerivedParams> derived;  // one per instance (= parameter block)
+
+  // network shape
+  int S = 0, U = 0, B = 0, Z = 0, R = 0;
+  std::vector<int> uni_list;    // order-1 reactions grouped by reactant
+  std::vector<int> bim_list;    // order-2 reactions, local index -> global
+  std::vector<int> zero_list;   // order-0 reactions
+  std::vector<int32_t> bim_table;
+  bool zero_two_products = false;
+
+  // device
+  int device = 0, n_sm = 152;
+  cudaStream_t stream = nullptr;
+  DevBuf<DevCtrl> ctrl;
+  DevCtrl* hctrl = nullptr;  // pinned mirror
+  DevBuf<DevInstance> dinst;
+  DevBuf<DevSpecies> dspecies;
+  DevBuf<DevUni> duni;
+  DevBuf<DevBim> dbim;
+  DevBuf<DevZero> dzero;
+  DevBuf<double> dcdf;
+  DevBuf<int32_t> dtable;
+  DevBuf<float> dgauss;
+  DevBuf<uint32_t> inst_step, inst_slot_base, zero_off;
+  DevBuf<unsigned long long> events, pending;
+  DevBuf<float4> state0, state1, scatter;
+  DevBuf<uint32_t> best, cell_count, cell_start, tile_sums;
+  DevBuf<DevPair> pairs;
+
+  std::vector<DevInstance> hinst;
+  uint32_t n_cells = 0, n_tiles = 0;
+  uint64_t capacity = 0;
+  uint32_t pair_cap = 0;
+  bool have_particles = false;
+  uint64_t target_step = 0;  // absolute step the enqueued work ends at
+  float cell_override = 0.0f;
+
+  cudaGraphExec_t graph1 = nullptr, graphN = nullptr;
+  LaunchShape shape{};
+
+  bool host_only = false;  // BD_DEVICE_NONE: parameters and grid only
+
+  bool diffuse_only() const { return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products; }
+  int n_inst() const { return (int)idesc.size(); }
+};
+
+namespace {
+
+void destroy_graphs(bd_system* h) {
+  if (h->graph1) cudaGraphExecDestroy(h->graph1);
+  if (h->graphN) cudaGraphExecDestroy(h->graphN);
+  h->graph1 = h->graphN = nullptr;
+}
+
+KParams make_params(bd_system* h) {
+  KParams p{};
+  p.state[0] = h->state0.p;
+  p.state[1] = h->state1.p;
+  p.scatter = h->scatter.p;
+  p.ctrl = h->ctrl.p;
+  p.inst = h->dinst.p;
+  p.species = h->dspecies.p;
+  p.uni = h->duni.p;
+  p.bim = h->dbim.p;
+  p.zero = h->dzero.p;
+  p.cdf = h->dcdf.p;
+  p.bim_table = h->dtable.p;
+  p.gauss = h->dgauss.p;
+  p.inst_step = h->inst_step.p;
+  p.inst_slot_base = h->inst_slot_base.p;
+  p.zero_off = h->zero_off.p;
+  p.cell_count = h->cell_count.p;
+  p.cell_start = h->cell_start.p;
+  p.tile_sums = h->tile_sums.p;
+  p.pairs = h->pairs.p;
+  p.best = h->best.p;
+  p.events = h->events.p;
+  p.pending = h->pending.p;
+  p.n_inst = (uint32_t)h->n_inst();
+  p.S = (uint32_t)h->S;
+  p.U = (uint32_t)h->U;
+  p.B = (uint32_t)h->B;
+  p.Z = (uint32_t)h->Z;
+  p.R = (uint32_t)h->R;
+  p.n_cells = h->n_cells;
+  p.n_tiles = h->n_tiles;
+  p.capacity = (uint32_t)h->capacity;
+  p.pair_cap = h->pair_cap;
+  p.prune_margin = 1e-3f;
+  return p;
+}
+
+bd_status build_graphs(bd_system* h) {
+  destroy_graphs(h);
+  const KParams p = make_params(h);
+  const bool table = h->cfg.normal_mode == BD_NORMALS_TABLE;
+  const Path path = h->diffuse_only() ? Path::kDiffuseOnly : Path::kSorted;
+  const bool has_zero = h->Z > 0, has_uni = h->U > 0, has_bim = h->B > 0;
+  for (int g = 0; g < 2; g++) {
+    const int nsteps = g == 0 ? 1 : kGraphBatch;
+    cudaGraph_t graph;
+    BD_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < nsteps; k++) enqueue_step(p, path, table, has_zero, has_uni, has_bim, h->shape, h->stream);
+    BD_CUDA(cudaStreamEndCapture(h->stream, &graph));
+    cudaGraphExec_t exec;
+    const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    BD_CUDA(e);
+    (g == 0 ? h->graph1 : h->graphN) = exec;
+  }
+  return BD_OK;
+}
+
+// Uniform grid of one instance: cells at least 1% wider than the largest
+// binding radius (so every reacting pair lies in the 27-cell neighbourhood),
+// otherwise sized for `occupancy` particles per cell.
+void choose_grid(bd_system* h, int k, uint64_t n_particles, DevInstance* I) {
+  const bd_instance_desc& d = h->idesc[k];
+  float rmax = 0.0f;
+  for (int b = 0; b < h->B; b++) rmax = std::max(rmax, h->derived[k].rx[h->bim_list[b]].bind_radius);
+  double L[3], vol = 1.0;
+  for (int a = 0; a < 3; a++) {
+    L[a] = (double)d.box_hi[a] - (double)d.box_lo[a];
+    vol *= L[a];
+  }
+  double cs;
+  const float want = h->cell_override > 0 ? h->cell_override : (d.cell_size > 0 ? d.cell_size : h->cfg.cell_size);
+  if (want > 0) {
+    cs = want;
+  } else {
+    const double occ = h->cfg.cell_occupancy > 0 ? h->cfg.cell_occupancy : 3.0;
+    cs = cbrt(occ * vol / (double)std::max<uint64_t>(n_particles, 1));
+  }
+  cs = std::max(cs, 1.01 * (double)rmax);
+  uint64_t total = 0;
+  for (int guard = 0; guard < 64; guard++) {
+    total = 1;
+    for (int a = 0; a < 3; a++) total *= (uint64_t)std::max(1.0, floor(L[a] / cs));
+    if (total <= (1ull << 28)) break;
+    cs *= 1.25;
+  }
+  for (int a = 0; a < 3; a++) {
+    I->lo[a] = d.box_lo[a];
+    I->hi[a] = d.box_hi[a];
+    I->dims[a] = (uint32_t)std::max(1.0, floor(L[a] / cs));
+    I->cell[a] = (float)(L[a] / I->dims[a]);
+    I->inv[a] = (float)I->dims[a] / (float)L[a];
+  }
+}
+
+bd_status validate_config(const bd_config* c) {
+  if (!c) return BD_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; a++)
+    if (!(c->box_hi[a] > c->box_lo[a])) return BD_ERR_INVALID_ARGUMENT;
+  if (!(c->dt > 0)) return BD_ERR_INVALID_ARGUMENT;
+  if (c->normal_mode != BD_NORMALS_BOXMULLER && c->normal_mode != BD_NORMALS_TABLE) return BD_ERR_INVALID_ARGUMENT;
+  return BD_OK;
+}
+
+bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int n, bd_handle* out) {
+  if (!out) return BD_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  bd_status st = validate_config(cfg);
+  if (st) return st;
+  if (n < 1 || (uint32_t)n > kMaxInstances) return BD_ERR_INVALID_ARGUMENT;
+  const bool host_only = cfg->device == BD_DEVICE_NONE;
+  int ndev = 0;
+  if (!host_only) {
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      g_last_error = "no CUDA device";
+      return BD_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return BD_ERR_INVALID_ARGUMENT;
+  }
+  bd_system* h = new bd_system();
+  h->host_only = host_only;
+  h->cfg = *cfg;
+  h->device = cfg->device;
+  if (inst) {
+    h->idesc.assign(inst, inst + n);
+    for (auto& d : h->idesc) {
+      for (int a = 0; a < 3; a++)
+        if (!(d.box_hi[a] > d.box_lo[a])) {
+          delete h;
+          return BD_ERR_INVALID_ARGUMENT;
+        }
+      if (!(d.d_scale > 0)) d.d_scale = 1.0f;
+      if (!(d.k2_scale > 0)) d.k2_scale = 1.0f;
+    }
+  } else {
+    bd_instance_desc d{};
+    memcpy(d.box_lo, cfg->box_lo, sizeof(d.box_lo));
+    memcpy(d.box_hi, cfg->box_hi, sizeof(d.box_hi));
+    d.seed = cfg->seed;
+    d.d_scale = d.k2_scale = 1.0f;
+    d.cell_size = 0.0f;
+    h->idesc.push_back(d);
+  }
+  if (host_only) {
+    *out = h;
+    return BD_OK;
+  }
+  if (!cuda_ok(cudaSetDevice(h->device), "cudaSetDevice") ||
+      !cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+      !cuda_ok(h->ctrl.alloc(1), "cudaMalloc ctrl") ||
+      !cuda_ok(cudaMallocHost((void**)&h->hctrl, sizeof(DevCtrl)), "cudaMallocHost")) {
+    bd_destroy(h);
+    return BD_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
+  h->shape.block_stream = 256;
+  h->shape.grid_stream = h->n_sm * 8;
+  h->shape.block_pairs = 256;
+  h->shape.grid_pairs = h->n_sm * 8;
+  memset(h->hctrl, 0, sizeof(DevCtrl));
+  cudaMemset(h->ctrl.p, 0, sizeof(DevCtrl));
+  *out = h;
+  return BD_OK;
+}
+
+template <class T>
+bd_status upload(DevBuf<T>& buf, const std::vector<T>& v, cudaStream_t s) {
+  BD_CUDA(buf.alloc(std::max<size_t>(v.size(), 1)));
+  if (!v.empty()) BD_CUDA(cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return BD_OK;
+}
+
+bd_status sync_ctrl(bd_system* h) {
+  BD_CUDA(cudaMemcpyAsync(h->hctrl, h->ctrl.p, sizeof(DevCtrl), cudaMemcpyDeviceToHost, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  return BD_OK;
+}
+
+bd_status push_ctrl(bd_system* h) {
+  BD_CUDA(cudaMemcpyAsync(h->ctrl.p, h->hctrl, sizeof(DevCtrl), cudaMemcpyHostToDevice, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  return BD_OK;
+}
+
+// (Re)allocate the particle-sized buffers for `cap` slots, keeping the
+// current state (n_slots records of the current buffer) in buffer 0.
+bd_status grow_particles(bd_system* h, uint64_t cap) {
+  if (cap > 0xFFFFFFF0ull) return BD_ERR_CAPACITY;
+  DevBuf<float4> s0, s1, sc;
+  DevBuf<uint32_t> best;
+  BD_CUDA(s0.alloc(cap));
+  BD_CUDA(s1.alloc(cap));
+  BD_CUDA(sc.alloc(cap));
+  BD_CUDA(best.alloc(cap));
+  BD_CUDA(cudaMemsetAsync(best.p, 0xFF, cap * sizeof(uint32_t), h->stream));
+  if (h->have_particles && h->hctrl->n_slots > 0) {
+    const float4* src = h->hctrl->cur ? h->state1.p : h->state0.p;
+    BD_CUDA(cudaMemcpyAsync(s0.p, src, (size_t)h->hctrl->n_slots * sizeof(float4), cudaMemcpyDeviceToDevice,
+                            h->stream));
+  }
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  h->state0.free();
+  h->state1.free();
+  h->scatter.free();
+  h->best.free();
+  h->state0 = s0;
+  h->state1 = s1;
+  h->scatter = sc;
+  h->best = best;
+  s0.p = s1.p = sc.p = nullptr;
+  best.p = nullptr;
+  h->hctrl->cur = 0;
+  h->capacity = cap;
+  return BD_OK;
+}
+
+bd_status grow_pairs(bd_system* h, uint32_t cap) {
+  BD_CUDA(h->pairs.alloc(cap));
+  h->pair_cap = cap;
+  return BD_OK;
+}
+
+// Grid, cell arrays and instance table for the current particle counts.
+bd_status setup_grid(bd_system* h, const std::vector<uint64_t>& counts) {
+  const int I = h->n_inst();
+  h->hinst.assign(I, DevInstance{});
+  uint64_t base = 0;
+  for (int k = 0; k < I; k++) {
+    DevInstance& D = h->hinst[k];
+    choose_grid(h, k, counts[k], &D);
+    D.cell_base = (uint32_t)base;
+    base += (uint64_t)D.dims[0] * D.dims[1] * D.dims[2];
+    D.key_lo = (uint32_t)(h->idesc[k].seed & 0xFFFFFFFFu);
+    D.key_hi = (uint32_t)(h->idesc[k].seed >> 32);
+    D.block = (uint32_t)k;
+    D.flags = kInstActive;
+  }
+  if (base > 0xFFFFFFF0ull) return BD_ERR_CAPACITY;
+  h->n_cells = (uint32_t)base;
+  h->n_tiles = (uint32_t)((base + kScanTile - 1) / kScanTile);
+  if (h->host_only) return BD_OK;
+  BD_CUDA(h->dinst.alloc(I));
+  BD_CUDA(cudaMemcpyAsync(h->dinst.p, h->hinst.data(), I * sizeof(DevInstance), cudaMemcpyHostToDevice, h->stream));
+  BD_CUDA(h->cell_count.alloc(h->n_cells));
+  BD_CUDA(cudaMemsetAsync(h->cell_count.p, 0, (size_t)h->n_cells * sizeof(uint32_t), h->stream));
+  BD_CUDA(h->cell_start.alloc((size_t)h->n_cells + 1));
+  BD_CUDA(cudaMemsetAsync(h->cell_start.p, 0, ((size_t)h->n_cells + 1) * sizeof(uint32_t), h->stream));
+  BD_CUDA(h->tile_sums.alloc(std::max<uint32_t>(h->n_tiles, 1)));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  return BD_OK;
+}
+
+bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, const uint64_t* counts) {
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  const int I = h->n_inst();
+  uint64_t n = 0;
+  for (int k = 0; k < I; k++) n += counts[k];
+  if (n > 0 && (!xyz4 || !species)) return BD_ERR_INVALID_ARGUMENT;
+  std::vector<float4> recs(n);
+  std::vector<uint32_t> slot_base(I, 0);
+  uint64_t i = 0;
+  for (int k = 0; k < I; k++) {
+    slot_base[k] = (uint32_t)i;
+    const bd_instance_desc& d = h->idesc[k];
+    for (uint64_t j = 0; j < counts[k]; j++, i++) {
+      const int s = species[i];
+      if (s < 0 || s >= h->S) return BD_ERR_INVALID_ARGUMENT;
+      float x = xyz4[4 * i], y = xyz4[4 * i + 1], z = xyz4[4 * i + 2];
+      if (!(x >= d.box_lo[0] && x <= d.box_hi[0] && y >= d.box_lo[1] && y <= d.box_hi[1] && z >= d.box_lo[2] &&
+            z <= d.box_hi[2]))
+        return BD_ERR_INVALID_ARGUMENT;
+      uint32_t w = ((uint32_t)k << 16) | (uint32_t)s;
+      float wf;
+      memcpy(&wf, &w, 4);
+      recs[i] = make_float4(x, y, z, wf);
+    }
+  }
+  std::vector<uint64_t> cvec(counts, counts + I);
+  bd_status st = setup_grid(h, cvec);
+  if (st) return st;
+  if (h->host_only) return BD_OK;
+  uint64_t cap = h->cfg.capacity ? h->cfg.capacity : std::max<uint64_t>(2 * n, 4096);
+  if (cap < n) cap = n;
+  h->have_particles = false;
+  memset(h->hctrl, 0, sizeof(DevCtrl));
+  st = grow_particles(h, cap);
+  if (st) return st;
+  uint32_t pc = h->cfg.pair_capacity ? h->cfg.pair_capacity : (uint32_t)std::max<uint64_t>(65536, cap / 32);
+  st = grow_pairs(h, pc);
+  if (st) return st;
+  if (n) BD_CUDA(cudaMemcpyAsync(h->state0.p, recs.data(), n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  std::vector<uint32_t> zeros(I, 0);
+  st = upload(h->inst_step, zeros, h->stream);
+  if (st) return st;
+  st = upload(h->inst_slot_base, slot_base, h->stream);
+  if (st) return st;
+  BD_CUDA(h->zero_off.alloc((size_t)I * h->Z + 1));
+  BD_CUDA(cudaMemsetAsync(h->zero_off.p, 0, ((size_t)I * h->Z + 1) * sizeof(uint32_t), h->stream));
+  BD_CUDA(h->events.alloc((size_t)I * std::max(h->R, 1)));
+  BD_CUDA(cudaMemsetAsync(h->events.p, 0, (size_t)I * std::max(h->R, 1) * sizeof(unsigned long long), h->stream));
+  BD_CUDA(h->pending.alloc((size_t)I * std::max(h->R, 1)));
+  BD_CUDA(cudaMemsetAsync(h->pending.p, 0, (size_t)I * std::max(h->R, 1) * sizeof(unsigned long long), h->stream));
+  memset(h->hctrl, 0, sizeof(DevCtrl));
+  h->hctrl->n_slots = (uint32_t)n;
+  st = push_ctrl(h);
+  if (st) return st;
+  h->have_particles = true;
+  h->target_step = 0;
+  return build_graphs(h);
+}
+
+}  // namespace
+
+// ======================================================================= ABI
+
+BD_API void bd_config_default(bd_config* c) {
+  if (!c) return;
+  memset(c, 0, sizeof(*c));
+  for (int a = 0; a < 3; a++) {
+    c->box_lo[a] = 0.0f;
+    c->box_hi[a] = 1.0f;
+  }
+  c->dt = 1e-3f;
+  c->seed = 1;
+  c->normal_mode = BD_NORMALS_BOXMULLER;
+}
+
+BD_API bd_status bd_create(const bd_config* cfg, bd_handle* out) { return create_common(cfg, nullptr, 1, out); }
+
+BD_API bd_status bd_create_ensemble(const bd_config* cfg, const bd_instance_desc* inst, int n, bd_handle* out) {
+  if (!inst) return BD_ERR_INVALID_ARGUMENT;
+  return create_common(cfg, inst, n, out);
+}
+
+BD_API bd_status bd_destroy(bd_handle h) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->host_only) cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  destroy_graphs(h);
+  h->ctrl.free();
+  if (h->hctrl) cudaFreeHost(h->hctrl);
+  h->dinst.free();
+  h->dspecies.free();
+  h->duni.free();
+  h->dbim.free();
+  h->dzero.free();
+  h->dcdf.free();
+  h->dtable.free();
+  h->dgauss.free();
+  h->inst_step.free();
+  h->inst_slot_base.free();
+  h->zero_off.free();
+  h->events.free();
+  h->pending.free();
+  h->state0.free();
+  h->state1.free();
+  h->scatter.free();
+  h->best.free();
+  h->cell_count.free();
+  h->cell_start.free();
+  h->tile_sums.free();
+  h->pairs.free();
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return BD_OK;
+}
+
+BD_API bd_status bd_add_species(bd_handle h, float D, int* id) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (!(D >= 0) || h->D.size() >= kMaxSpecies) return BD_ERR_INVALID_ARGUMENT;
+  h->D.push_back(D);
+  if (id) *id = (int)h->D.size() - 1;
+  return BD_OK;
+}
+
+BD_API bd_status bd_add_reaction(bd_handle h, int order, const int reactants[2], const int products[2], float rate,
+                                 int* id) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (order < 0 || order > 2) return BD_ERR_INVALID_ARGUMENT;
+  if (rate < 0) return BD_ERR_NEGATIVE_RATE;
+  const int S = (int)h->D.size();
+  ReactionDef r;
+  r.order = order;
+  r.rate = rate;
+  for (int k = 0; k < 2; k++) {
+    r.reactants[k] = reactants ? reactants[k] : -1;
+    r.products[k] = products ? products[k] : -1;
+  }
+  for (int k = 0; k < order; k++)
+    if (r.reactants[k] < 0 || r.reactants[k] >= S) return BD_ERR_INVALID_ARGUMENT;
+  for (int k = order; k < 2; k++) r.reactants[k] = -1;
+  if (r.products[0] < 0 && r.products[1] >= 0) std::swap(r.products[0], r.products[1]);
+  for (int k = 0; k < 2; k++)
+    if (r.products[k] >= S) return BD_ERR_INVALID_ARGUMENT;
+  r.nprod = (r.products[0] >= 0) + (r.products[1] >= 0);
+  if (order == 0 && r.nprod == 0) return BD_ERR_INVALID_ARGUMENT;
+  h->rx.push_back(r);
+  if (id) *id = (int)h->rx.size() - 1;
+  return BD_OK;
+}
+
+BD_API bd_status bd_set_product_placement(bd_handle h, int rxn, int kind, float param) {
+  if (!h || rxn < 0 || rxn >= (int)h->rx.size()) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (kind < BD_PP_DEFAULT || kind > BD_PP_OFFSET0) return BD_ERR_INVALID_ARGUMENT;
+  h->rx[rxn].pp_kind = kind;
+  h->rx[rxn].pp_param = param;
+  return BD_OK;
+}
+
+BD_API bd_status bd_set_reaction_probability(bd_handle h, int rxn, float prob) {
+  if (!h || rxn < 0 || rxn >= (int)h->rx.size()) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (h->rx[rxn].order != 2 || !(prob >= 0.0f && prob <= 1.0f)) return BD_ERR_INVALID_ARGUMENT;
+  h->rx[rxn].user_prob = prob;
+  return BD_OK;
+}
+
+BD_API bd_status bd_finalize(bd_handle h) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (h->D.empty()) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->host_only) BD_CUDA(cudaSetDevice(h->device));
+  const int I = h->n_inst();
+  h->S = (int)h->D.size();
+  h->R = (int)h->rx.size();
+  bd_status first = BD_OK;
+  h->derived.clear();
+  for (int k = 0; k < I; k++) {
+    const bd_instance_desc& d = h->idesc[k];
+    const float vol = (d.box_hi[0] - d.box_lo[0]) * (d.box_hi[1] - d.box_lo[1]) * (d.box_hi[2] - d.box_lo[2]);
+    h->derived.push_back(derive_params(h->D, h->rx, h->cfg.dt, vol, d.d_scale, d.k2_scale));
+    if (!first && h->derived.back().status) {
+      first = h->derived.back().status;
+      g_last_error = h->derived.back().message;
+    }
+  }
+  // fatal setup errors leave the handle unfinalized
+  if (first == BD_ERR_NEGATIVE_RATE || first == BD_ERR_ZERO_DIFFUSION || first == BD_ERR_ILLEGAL_UNBIND) return first;
+
+  // network shape
+  h->uni_list.clear();
+  h->bim_list.clear();
+  h->zero_list.clear();
+  h->zero_two_products = false;
+  for (int s = 0; s < h->S; s++)
+    for (int r = 0; r < h->R; r++)
+      if (h->rx[r].order == 1 && h->rx[r].reactants[0] == s) h->uni_list.push_back(r);
+  for (int r = 0; r < h->R; r++) {
+    if (h->rx[r].order == 2) h->bim_list.push_back(r);
+    if (h->rx[r].order == 0) {
+      h->zero_list.push_back(r);
+      if (h->rx[r].nprod == 2) h->zero_two_products = true;
+    }
+  }
+  h->U = (int)h->uni_list.size();
+  h->B = (int)h->bim_list.size();
+  h->Z = (int)h->zero_list.size();
+  const int S = h->S, U = h->U, B = h->B, Z = h->Z;
+
+  // pair table: the last reaction listed for a pair wins (particleSystem.cpp:656-669);
+  // a reaction with zero binding radius never fires
+  h->bim_table.assign((size_t)S * S, -1);
+  for (int b = 0; b < B; b++) {
+    const ReactionDef& r = h->rx[h->bim_list[b]];
+    bool any = false;
+    for (int k = 0; k < I; k++) any |= h->derived[k].rx[h->bim_list[b]].bind_r2 > 0;
+    const int v = any ? b : -1;
+    h->bim_table[(size_t)r.reactants[0] * S + r.reactants[1]] = v;
+    h->bim_table[(size_t)r.reactants[1] * S + r.reactants[0]] = v;
+  }
+
+  std::vector<DevSpecies> sp((size_t)I * S);
+  std::vector<DevUni> un((size_t)I * U);
+  std::vector<DevBim> bi((size_t)I * B);
+  std::vector<DevZero> ze((size_t)I * Z);
+  std::vector<double> cdf;
+  for (int k = 0; k < I; k++) {
+    const DerivedParams& P = h->derived[k];
+    int u = 0;
+    for (int s = 0; s < S; s++) {
+      DevSpecies& ds = sp[(size_t)k * S + s];
+      ds.sigma = P.sigma[s];
+      ds.uni_begin = (uint32_t)u;
+      ds.uni_count = 0;
+      ds.max_r = 0.0f;
+      while (u < U && h->rx[h->uni_list[u]].reactants[0] == s) {
+        const int r = h->uni_list[u];
+        DevUni& du = un[(size_t)k * U + u];
+        du.prob = P.rx[r].prob;
+        du.prod0 = h->rx[r].products[0];
+        du.prod1 = h->rx[r].products[1];
+        du.off0 = P.rx[r].off[0];
+        du.off1 = P.rx[r].off[1];
+        du.rxn = (uint32_t)r;
+        ds.uni_count++;
+        u++;
+      }
+      for (int s2 = 0; s2 < S; s2++) {
+        const int b = h->bim_table[(size_t)s * S + s2];
+        if (b >= 0) ds.max_r = std::max(ds.max_r, P.rx[h->bim_list[b]].bind_radius);
+      }
+    }
+    for (int b = 0; b < B; b++) {
+      const int r = h->bim_list[b];
+      DevBim& db = bi[(size_t)k * B + b];
+      db.r2 = P.rx[r].bind_r2;
+      db.prob = P.rx[r].prob;
+      db.x = P.rx[r].x;
+      db.omx = P.rx[r].omx;
+      db.react0 = h->rx[r].reactants[0];
+      db.prod0 = h->rx[r].products[0];
+      db.prod1 = h->rx[r].products[1];
+      db.off0 = P.rx[r].off[0];
+      db.off1 = P.rx[r].off[1];
+      db.rxn = (uint32_t)r;
+    }
+    for (int z = 0; z < Z; z++) {
+      const int r = h->zero_list[z];
+      DevZero& dz = ze[(size_t)k * Z + z];
+      dz.prod0 = h->rx[r].products[0];
+      dz.prod1 = h->rx[r].products[1];
+      dz.cdf_off = (uint32_t)cdf.size();
+      dz.cdf_len = (uint32_t)P.cdf[r].size();
+      dz.kmin = P.cdf_kmin[r];
+      dz.rxn = (uint32_t)r;
+      cdf.insert(cdf.end(), P.cdf[r].begin(), P.cdf[r].end());
+    }
+  }
+  if (h->host_only) {
+    h->finalized = true;
+    return first;
+  }
+  std::vector<float> gauss(4096);
+  gauss_quantiles(gauss.data(), 4096);
+  bd_status st;
+  if ((st = upload(h->dspecies, sp, h->stream)) || (st = upload(h->duni, un, h->stream)) ||
+      (st = upload(h->dbim, bi, h->stream)) || (st = upload(h->dzero, ze, h->stream)) ||
+      (st = upload(h->dcdf, cdf, h->stream)) || (st = upload(h->dtable, h->bim_table, h->stream)) ||
+      (st = upload(h->dgauss, gauss, h->stream)))
+    return st;
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  h->finalized = true;
+  return first;
+}
+
+BD_API bd_status bd_get_counts(bd_handle h, int* n_species, int* n_reactions) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (n_species) *n_species = (int)h->D.size();
+  if (n_reactions) *n_reactions = (int)h->rx.size();
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_instance_reaction_info(bd_handle h, int inst, int rxn, bd_reaction_info* out) {
+  if (!h || !out || rxn < 0 || rxn >= (int)h->rx.size() || inst < 0 || inst >= h->n_inst())
+    return BD_ERR_INVALID_ARGUMENT;
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  const ReactionDef& r = h->rx[rxn];
+  const DerivedReaction& d = h->derived[inst].rx[rxn];
+  memset(out, 0, sizeof(*out));
+  out->order = r.order;
+  out->nprod = r.nprod;
+  for (int k = 0; k < 2; k++) {
+    out->reactants[k] = r.reactants[k];
+    out->products[k] = r.products[k];
+    out->product_offsets[k] = d.off[k];
+  }
+  out->rate = r.rate;
+  out->prob = d.prob;
+  out->bind_radius = d.bind_radius;
+  out->unbind_radius = d.unbind_radius;
+  out->geminate_prob = d.gem_prob;
+  out->reverse = d.reverse;
+  out->flags = d.flags;
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_reaction_info(bd_handle h, int rxn, bd_reaction_info* out) {
+  return bd_get_instance_reaction_info(h, 0, rxn, out);
+}
+
+BD_API bd_status bd_set_particles(bd_handle h, const float* xyz4, const int* species, size_t n) {
+  if (!h || h->n_inst() != 1) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->host_only) BD_CUDA(cudaSetDevice(h->device));
+  const uint64_t c = n;
+  return upload_particles(h, xyz4, species, &c);
+}
+
+BD_API bd_status bd_set_ensemble_particles(bd_handle h, const float* xyz4, const int* species, const uint64_t* counts,
+                                           int n_instances) {
+  if (!h || !counts || n_instances != h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->host_only) BD_CUDA(cudaSetDevice(h->device));
+  return upload_particles(h, xyz4, species, counts);
+}
+
+BD_API bd_status bd_step(bd_handle h, int nsteps) {
+  if (!h || nsteps < 0) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  if (!h->have_particles) return BD_ERR_NOT_FINALIZED;
+  BD_CUDA(cudaSetDevice(h->device));
+  if (!h->graph1) {
+    const bd_status st = build_graphs(h);
+    if (st) return st;
+  }
+  int left = nsteps;
+  while (left >= kGraphBatch) {
+    BD_CUDA(cudaGraphLaunch(h->graphN, h->stream));
+    left -= kGraphBatch;
+  }
+  while (left-- > 0) BD_CUDA(cudaGraphLaunch(h->graph1, h->stream));
+  h->target_step += (uint64_t)nsteps;
+  return BD_OK;
+}
+
+BD_API bd_status bd_synchronize(bd_handle h) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->have_particles) return BD_OK;
+  BD_CUDA(cudaSetDevice(h->device));
+  for (int attempt = 0; attempt < 64; attempt++) {
+    bd_status st = sync_ctrl(h);
+    if (st) return st;
+    DevCtrl& c = *h->hctrl;
+    if (c.status == 0) {
+      if (c.step >= h->target_step) break;
+      // a previous failed step stopped the queue; replay the rest
+    } else {
+      if (c.status & (kStatBounds | kStatTimeout)) {
+        g_last_error = "device reported an inconsistent state";
+        return (c.status & kStatTimeout) ? BD_ERR_TIMEOUT : BD_ERR_DEVICE_STATE;
+      }
+      if (c.status & kStatCapacity) {
+        uint64_t need = std::max<uint64_t>(c.n_sorted, (uint64_t)c.n_slots + c.n_virtual);
+        uint64_t cap = std::max<uint64_t>(2 * h->capacity, need + need / 2 + 1024);
+        st = grow_particles(h, cap);
+        if (st) return st;
+      }
+      if (c.status & kStatPairs) {
+        uint64_t cap = std::max<uint64_t>(2ull * h->pair_cap, (uint64_t)c.n_pairs + c.n_pairs / 2 + 1024);
+        if (cap > 0x7FFFFFFFull) return BD_ERR_CAPACITY;
+        st = grow_pairs(h, (uint32_t)cap);
+        if (st) return st;
+      }
+      BD_CUDA(cudaMemsetAsync(h->cell_count.p, 0, (size_t)h->n_cells * sizeof(uint32_t), h->stream));
+      BD_CUDA(cudaMemsetAsync(h->pending.p, 0, h->pending.n * sizeof(unsigned long long), h->stream));
+      c.status = 0;
+      c.n_pairs = 0;
+      c.n_virtual = 0;
+      st = push_ctrl(h);
+      if (st) return st;
+      st = build_graphs(h);
+      if (st) return st;
+    }
+    const uint64_t left = h->target_step - c.step;
+    if (left == 0) break;
+    h->target_step = c.step;
+    st = bd_step(h, (int)left);
+    if (st) return st;
+  }
+  const DevCtrl& c = *h->hctrl;
+  if (c.step < h->target_step) return BD_ERR_CAPACITY;
+  if ((uint64_t)c.n_slots - c.deaths_last == 0) return BD_ERR_EMPTY;
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_step(bd_handle h, uint64_t* step) {
+  if (!h || !step) return BD_ERR_INVALID_ARGUMENT;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  *step = h->hctrl->step;
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_count(bd_handle h, uint64_t* n) {
+  if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->have_particles) {
+    *n = 0;
+    return BD_OK;
+  }
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  *n = (uint64_t)h->hctrl->n_slots - h->hctrl->deaths_last;
+  return BD_OK;
+}
+
+namespace {
+bd_status read_slots(bd_system* h, std::vector<float4>* out) {
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const uint32_t n = h->hctrl->n_slots;
+  out->resize(n);
+  const float4* src = h->hctrl->cur ? h->state1.p : h->state0.p;
+  if (n) BD_CUDA(cudaMemcpy(out->data(), src, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost));
+  return BD_OK;
+}
+}  // namespace
+
+BD_API bd_status bd_get_particles(bd_handle h, float* xyz4, int* species, size_t cap, size_t* n) {
+  return bd_get_instance_particles(h, -1, xyz4, species, cap, n);
+}
+
+BD_API bd_status bd_get_instance_particles(bd_handle h, int inst, float* xyz4, int* species, size_t cap,
+                                           size_t* n) {
+  if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
+  if (inst >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  *n = 0;
+  if (!h->have_particles) return BD_OK;
+  std::vector<float4> slots;
+  bd_status st = read_slots(h, &slots);
+  if (st) return st;
+  size_t k = 0;
+  for (const float4& r : slots) {
+    uint32_t w;
+    memcpy(&w, &r.w, 4);
+    if (w == kDead) continue;
+    if (inst >= 0 && (int)(w >> 16) != inst) continue;
+    if (k < cap) {
+      if (xyz4) {
+        xyz4[4 * k] = r.x;
+        xyz4[4 * k + 1] = r.y;
+        xyz4[4 * k + 2] = r.z;
+        xyz4[4 * k + 3] = 1.0f;
+      }
+      if (species) species[k] = (int)(w & 0xFFFFu);
+    }
+    k++;
+  }
+  *n = k;
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_state_pointer(bd_handle h, void** dev_records, uint64_t* n_slots) {
+  if (!h || !dev_records || !n_slots) return BD_ERR_INVALID_ARGUMENT;
+  *dev_records = nullptr;
+  *n_slots = 0;
+  if (!h->have_particles) return BD_OK;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  *dev_records = h->hctrl->cur ? (void*)h->state1.p : (void*)h->state0.p;
+  *n_slots = h->hctrl->n_slots;
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_instance_counts(bd_handle h, uint64_t* counts, int n_instances) {
+  if (!h || !counts || n_instances != h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->have_particles) {
+    for (int k = 0; k < n_instances; k++) counts[k] = 0;
+    return BD_OK;
+  }
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  DevBuf<unsigned long long> d;
+  BD_CUDA(d.alloc(n_instances));
+  BD_CUDA(cudaMemsetAsync(d.p, 0, n_instances * sizeof(unsigned long long), h->stream));
+  enqueue_instance_counts(make_params(h), d.p, h->stream);
+  BD_CUDA(cudaGetLastError());
+  BD_CUDA(cudaMemcpyAsync(counts, d.p, n_instances * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  d.free();
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_event_counts(bd_handle h, uint64_t* counts, int n) {
+  if (!h || !counts || n < 0) return BD_ERR_INVALID_ARGUMENT;
+  for (int r = 0; r < n; r++) counts[r] = 0;
+  if (!h->have_particles) return BD_OK;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const int I = h->n_inst(), R = std::max(h->R, 1);
+  std::vector<unsigned long long> ev((size_t)I * R);
+  BD_CUDA(cudaMemcpy(ev.data(), h->events.p, ev.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < I; k++)
+    for (int r = 0; r < std::min(n, h->R); r++) counts[r] += ev[(size_t)k * R + r];
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_stage_times(bd_handle h, float* ms, int n) {
+  if (!h || !ms) return BD_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < n; k++) ms[k] = 0.0f;
+  return BD_OK;
+}
+
+BD_API bd_status bd_debug_get_slots(bd_handle h, float* xyz4, uint32_t* w, size_t cap, size_t* n) {
+  if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
+  *n = 0;
+  if (!h->have_particles) return BD_OK;
+  std::vector<float4> slots;
+  bd_status st = read_slots(h, &slots);
+  if (st) return st;
+  *n = slots.size();
+  for (size_t i = 0; i < slots.size() && i < cap; i++) {
+    if (xyz4) {
+      xyz4[4 * i] = slots[i].x;
+      xyz4[4 * i + 1] = slots[i].y;
+      xyz4[4 * i + 2] = slots[i].z;
+      xyz4[4 * i + 3] = 0.0f;
+    }
+    if (w) memcpy(&w[i], &slots[i].w, 4);
+  }
+  return BD_OK;
+}
+
+BD_API bd_status bd_debug_get_cells(bd_handle h, uint32_t* start, size_t cap, size_t* ncells) {
+  if (!h || !ncells) return BD_ERR_INVALID_ARGUMENT;
+  *ncells = h->n_cells;
+  if (!h->have_particles) return BD_OK;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  if (start) {
+    const size_t m = std::min<size_t>(cap, (size_t)h->n_cells + 1);
+    BD_CUDA(cudaMemcpy(start, h->cell_start.p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  }
+  return BD_OK;
+}
+
+BD_API bd_status bd_debug_get_pairs(bd_handle h, uint32_t* quads, size_t cap, size_t* n) {
+  if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
+  *n = 0;
+  if (!h->have_particles) return BD_OK;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const uint32_t K = h->hctrl->n_pairs_last;
+  *n = K;
+  if (quads && K) {
+    std::vector<DevPair> v(K);
+    BD_CUDA(cudaMemcpy(v.data(), h->pairs.p, K * sizeof(DevPair), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < K && k < cap; k++) {
+      quads[4 * k] = v[k].i;
+      quads[4 * k + 1] = v[k].j;
+      quads[4 * k + 2] = (uint32_t)h->bim_list[v[k].b & 0xFFFFu];
+      quads[4 * k + 3] = v[k].state == 1 ? 1u : 0u;
+    }
+  }
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_grid(bd_handle h, int inst, uint32_t dims[3], float cell[3], float inv[3]) {
+  if (!h || inst < 0) return BD_ERR_INVALID_ARGUMENT;
+  if (h->hinst.empty()) return BD_ERR_NOT_FINALIZED;
+  if (inst >= (int)h->hinst.size()) return BD_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; a++) {
+    if (dims) dims[a] = h->hinst[inst].dims[a];
+    if (cell) cell[a] = h->hinst[inst].cell[a];
+    if (inv) inv[a] = h->hinst[inst].inv[a];
+  }
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_poisson_cdf(bd_handle h, int inst, int rxn, double* cdf, size_t cap, int* kmin, size_t* len) {
+  if (!h || inst < 0 || inst >= h->n_inst() || rxn < 0 || rxn >= (int)h->rx.size()) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  const std::vector<double>& v = h->derived[inst].cdf[rxn];
+  if (len) *len = v.size();
+  if (kmin) *kmin = h->derived[inst].cdf_kmin[rxn];
+  if (cdf)
+    for (size_t k = 0; k < v.size() && k < cap; k++) cdf[k] = v[k];
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_species_d(bd_handle h, int inst, int species, float* D) {
+  if (!h || !D || inst < 0 || inst >= h->n_inst() || species < 0 || species >= (int)h->D.size())
+    return BD_ERR_INVALID_ARGUMENT;
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  *D = h->derived[inst].D[species];
+  return BD_OK;
+}
+
+BD_API bd_status bd_set_cell_size(bd_handle h, float cell_size) {
+  if (!h || !(cell_size >= 0)) return BD_ERR_INVALID_ARGUMENT;
+  h->cell_override = cell_size;
+  return BD_OK;
+}
+
+BD_API double bd_numrxnrate(double step, double a, double b) { return numrxnrate(step, a, b); }
+BD_API double bd_actrxnrate(double step, double a) { return actrxnrate(step, a); }
+BD_API double bd_bindingradius(double rate, double dt, double difc, double b, int rel) {
+  return bindingradius(rate, dt, difc, b, rel);
+}
+BD_API double bd_unbindingradius(double pgem, double dt, double difc, double a) {
+  return unbindingradius(pgem, dt, difc, a);
+}
+BD_API int bd_gauss_table(float* out, int n) {
+  if (!out || n <= 0 || (n & 1)) return -1;
+  gauss_quantiles(out, n);
+  return n;
+}
+
+BD_API const char* bd_status_string(bd_status s) {
+  switch (s) {
+    case BD_OK: return "ok";
+    case BD_ERR_NEGATIVE_RATE: return "negative reaction rate";
+    case BD_ERR_STATE_DEPENDENT: return "state-dependent reaction probability";
+    case BD_ERR_ZERO_DIFFUSION: return "diffusion coefficients sum to zero";
+    case BD_ERR_ILLEGAL_UNBIND: return "illegal input for the unbinding radius";
+    case BD_ERR_PGEM_UNATTAINABLE: return "geminate probability unattainable";
+    case BD_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case BD_ERR_NOT_FINALIZED: return "not finalized / no particles";
+    case BD_ERR_ALREADY_FINALIZED: return "already finalized";
+    case BD_ERR_CAPACITY: return "capacity exceeded";
+    case BD_ERR_EMPTY: return "no particles left";
+    case BD_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
+    case BD_ERR_TIMEOUT: return "device wait timed out";
+    case BD_ERR_NO_DEVICE: return "no CUDA device";
+    case BD_ERR_DEVICE_STATE: return "device state check failed";
+    case BD_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+BD_API const char* bd_version(void) { return "gpusmoldyn-gb300 0.1 (sm_103a)"; }

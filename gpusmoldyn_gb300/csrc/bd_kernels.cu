@@ -1,0 +1,701 @@
+// bd_kernels.cu -- the per-timestep kernels of the Brownian-dynamics step.
+//
+// Sorted path (any first- or second-order reaction, or an ensemble), one
+// step = 7 or 8 launches, no host synchronisation, all counts on the device:
+//
+//   k_zeroth    1 CTA      Poisson birth counts of the zeroth-order reactions
+//                          (zeroReact + poisrandF on the host in the
+//                          reference, reaction_cpu.cpp:36-63, stats.cpp:234-275)
+//   k_count     streaming  diffuse + reflect + first-order reactions + cell key,
+//                          warp-aggregated cell histogram; writes nothing else
+//                          (diffuse, uniReact, adjustPositions, calcHashD:
+//                          particles_kernel.cu:61-95, 127-207,
+//                          reaction_kernel.cuh:263-342)
+//   k_scan_*    3 launches exclusive scan of the cell histogram = cell starts
+//                          (replaces RadixSort's 5 passes + CUDPP scans,
+//                          radixsort.cu:1045-1143, and the cellStart memset)
+//   k_scatter   streaming  recomputes k_count's records (counter-based RNG makes
+//                          them identical) and scatters each into its cell;
+//                          dead particles get no slot, births get one
+//                          (compactPosAndTypeD, particles_kernel.cu:98-123)
+//   k_pairs     streaming  canonical order inside each cell + pair search over
+//                          the neighbour cells within the binding radius
+//                          (reorderDataAndFindCellStartD, collideD, collideCell:
+//                          particles_kernel.cu:212-272, 318-497)
+//   k_match     1 CTA      one reaction per particle (greedy matching in pair
+//                          order), product placement, counters, commit
+//                          (bimReact, resetNonInteracting: reaction_kernel.cuh:
+//                          202-258, particles_kernel.cu:499-508)
+//
+// HBM traffic per particle-step: k_count R16, k_scatter R16 + W16, k_pairs
+// R16 + W16 = 80 B, plus 4-12 B per cell for the histogram and the starts.
+//
+// Diffusion-only path (no first- or second-order reaction, one instance):
+// k_diffuse updates the records in place (R16 + W16) and zeroth-order births
+// are appended by k_append.
+#include "bd_device.cuh"
+#include "bd_kernels.h"
+
+namespace bd {
+namespace {
+
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;
+constexpr uint32_t kFree = 0xFFFFFFFFu;
+constexpr uint32_t kMatched = 0xFFFFFFFEu;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ uint32_t ld_u32(const uint32_t* p) { return __ldcg(p); }
+
+// ctrl words are written by earlier kernels and read here through L2.
+__device__ __forceinline__ uint32_t ctrl_status_warp(const DevCtrl* c) {
+  uint32_t s = 0;
+  if (lane_id() == 0) s = ld_u32(&c->status);
+  return __shfl_sync(kFull, s, 0);
+}
+
+__device__ __forceinline__ const float4* cur_state(const KParams& p, uint32_t cur) {
+  return cur ? p.state[1] : p.state[0];
+}
+__device__ __forceinline__ float4* next_state(const KParams& p, uint32_t cur) {
+  return cur ? p.state[0] : p.state[1];
+}
+
+struct Out2 {
+  float4 r[2];
+  uint32_t key[2];
+  int n;
+};
+
+__device__ __forceinline__ uint32_t word_of(const U4& c, uint32_t k) {
+  switch (k & 3u) {
+    case 0: return c.x;
+    case 1: return c.y;
+    case 2: return c.z;
+    default: return c.w;
+  }
+}
+
+// Advance the record in slot i by one step: diffusion, reflection and the
+// first successful first-order reaction (reaction_kernel.cuh:303-341: coins
+// in list order, decay when the first product is absent, a second product
+// becomes a birth).  kCount adds fired reactions to the event counters.
+template <bool kTable, bool kCount>
+__device__ __forceinline__ void advance_real(const KParams& p, const float4* __restrict__ cur, uint32_t i,
+                                             Out2& o) {
+  o.n = 0;
+  const float4 rec = cur[i];
+  const uint32_t w = rec_w(rec);
+  if (w == kDead) return;
+  const uint32_t inst = w >> 16, sp = w & 0xFFFFu;
+  const DevInstance& I = p.inst[inst];
+  const uint32_t flags = I.flags;
+  if (flags & kInstRemoved) return;
+  if ((flags & kInstFrozen) || !(flags & kInstActive)) {
+    o.r[0] = rec;
+    o.key[0] = cell_key(I, rec.x, rec.y, rec.z);
+    o.n = 1;
+    return;
+  }
+  const uint32_t local = i - p.inst_slot_base[inst];
+  const uint32_t t = p.inst_step[inst];
+  const uint32_t k0 = I.key_lo, k1 = I.key_hi;
+  const DevSpecies S = p.species[I.block * p.S + sp];
+
+  const U4 rn = philox(U4{local, t, kTagDiffuse, 0u}, k0, k1);
+  float g0, g1, g2;
+  normals3<kTable>(rn, p.gauss, g0, g1, g2);
+  float x = reflect(__fmaf_rn(S.sigma, g0, rec.x), I.lo[0], I.hi[0]);
+  float y = reflect(__fmaf_rn(S.sigma, g1, rec.y), I.lo[1], I.hi[1]);
+  float z = reflect(__fmaf_rn(S.sigma, g2, rec.z), I.lo[2], I.hi[2]);
+  uint32_t species = sp;
+  int n = 1;
+
+  U4 coins{0u, 0u, 0u, 0u};
+  for (uint32_t k = 0; k < S.uni_count; ++k) {
+    if ((k & 3u) == 0) coins = philox(U4{local, t, kTagUniCoin | (k >> 2), 0u}, k0, k1);
+    const DevUni& u = p.uni[I.block * p.U + S.uni_begin + k];
+    if (u32_to_unit(word_of(coins, k)) < u.prob) {
+      if (kCount) atomicAdd(&p.pending[(size_t)inst * p.R + u.rxn], 1ull);
+      if (u.prod0 < 0) return;  // decay: no record
+      species = (uint32_t)u.prod0;
+      if (u.prod1 >= 0) {
+        float bx = x, by = y, bz = z;
+        if (u.off0 != 0.0f || u.off1 != 0.0f) {
+          float dx, dy, dz;
+          unit_vector(local, t, kTagUniDir, 0u, k0, k1, dx, dy, dz);
+          bx = reflect(__fmaf_rn(u.off1, dx, x), I.lo[0], I.hi[0]);
+          by = reflect(__fmaf_rn(u.off1, dy, y), I.lo[1], I.hi[1]);
+          bz = reflect(__fmaf_rn(u.off1, dz, z), I.lo[2], I.hi[2]);
+          x = reflect(__fmaf_rn(u.off0, dx, x), I.lo[0], I.hi[0]);
+          y = reflect(__fmaf_rn(u.off0, dy, y), I.lo[1], I.hi[1]);
+          z = reflect(__fmaf_rn(u.off0, dz, z), I.lo[2], I.hi[2]);
+        }
+        o.r[1] = make_float4(bx, by, bz, __uint_as_float(pack_w(inst, (uint32_t)u.prod1)));
+        o.key[1] = cell_key(I, bx, by, bz);
+        n = 2;
+      }
+      break;
+    }
+  }
+  o.r[0] = make_float4(x, y, z, __uint_as_float(pack_w(inst, species)));
+  o.key[0] = cell_key(I, x, y, z);
+  o.n = n;
+}
+
+// Zeroth-order birth number v of this step: uniform position in the box
+// (reaction_cpu.cpp:44-60 with randPos, particleSystem.h:115-120).
+__device__ __forceinline__ void advance_virtual(const KParams& p, uint32_t v, Out2& o) {
+  const uint32_t nz = p.n_inst * p.Z;
+  // entry e with zero_off[e] <= v < zero_off[e + 1]
+  uint32_t lo = 0, hi = nz;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (p.zero_off[mid] <= v) lo = mid;
+    else hi = mid;
+  }
+  const uint32_t inst = lo / p.Z, zr = lo % p.Z;
+  const uint32_t k_local = v - p.zero_off[inst * p.Z];
+  const DevInstance& I = p.inst[inst];
+  const uint32_t t = p.inst_step[inst];
+  const U4 r = philox(U4{k_local, t, kTagZeroPos, 0u}, I.key_lo, I.key_hi);
+  const float x = fminf(__fmaf_rn(u24_to_unit(r.x), __fsub_rn(I.hi[0], I.lo[0]), I.lo[0]), I.hi[0]);
+  const float y = fminf(__fmaf_rn(u24_to_unit(r.y), __fsub_rn(I.hi[1], I.lo[1]), I.lo[1]), I.hi[1]);
+  const float z = fminf(__fmaf_rn(u24_to_unit(r.z), __fsub_rn(I.hi[2], I.lo[2]), I.lo[2]), I.hi[2]);
+  const DevZero& Zr = p.zero[I.block * p.Z + zr];
+  const uint32_t key = cell_key(I, x, y, z);
+  o.r[0] = make_float4(x, y, z, __uint_as_float(pack_w(inst, (uint32_t)Zr.prod0)));
+  o.key[0] = key;
+  o.n = 1;
+  if (Zr.prod1 >= 0) {
+    o.r[1] = make_float4(x, y, z, __uint_as_float(pack_w(inst, (uint32_t)Zr.prod1)));
+    o.key[1] = key;
+    o.n = 2;
+  }
+}
+
+// Lanes with equal keys add their count with one atomic.
+__device__ __forceinline__ void warp_count(uint32_t* cnt, uint32_t key) {
+  const uint32_t peers = __match_any_sync(kFull, key);
+  if (key != kNoKey && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&cnt[key], (uint32_t)__popc(peers));
+}
+
+// Lanes with equal keys take consecutive places of their cell with one
+// atomic; the count goes back to zero as the cell fills.
+__device__ __forceinline__ uint32_t warp_claim(uint32_t* cnt, uint32_t key) {
+  const uint32_t peers = __match_any_sync(kFull, key);
+  const int leader = __ffs(peers) - 1;
+  const uint32_t rank = __popc(peers & ((1u << lane_id()) - 1u));
+  uint32_t old = 0;
+  if (key != kNoKey && lane_id() == (uint32_t)leader) old = atomicSub(&cnt[key], (uint32_t)__popc(peers));
+  old = __shfl_sync(kFull, old, leader);
+  return old - 1u - rank;
+}
+
+template <int kThreads>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sums[kThreads / 32];
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t n = __shfl_up_sync(kFull, incl, d);
+    if (lane >= (uint32_t)d) incl += n;
+  }
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < kThreads / 32 ? warp_sums[lane] : 0u;
+    uint32_t si = s;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t n = __shfl_up_sync(kFull, si, d);
+      if (lane >= (uint32_t)d) si += n;
+    }
+    if (lane < kThreads / 32) warp_sums[lane] = si - s;
+    const uint32_t tot = __shfl_sync(kFull, si, 31);
+    if (lane == 0) *total = tot;
+  }
+  __syncthreads();
+  const uint32_t r = warp_sums[warp] + incl - v;
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------- kernels
+
+__global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
+  __shared__ uint32_t s_total;
+  DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;
+  const uint32_t nz = p.n_inst * p.Z;
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < nz; base += 1024) {
+    const uint32_t e = base + threadIdx.x;
+    uint32_t cnt = 0;
+    if (e < nz) {
+      const uint32_t inst = e / p.Z, zr = e % p.Z;
+      const DevInstance& I = p.inst[inst];
+      if ((I.flags & kInstActive) && !(I.flags & (kInstFrozen | kInstRemoved))) {
+        const DevZero& Zr = p.zero[I.block * p.Z + zr];
+        const U4 r = philox(U4{zr, p.inst_step[inst], kTagZeroCount, 0u}, I.key_lo, I.key_hi);
+        const double u = u53_to_unit(r.x, r.y);
+        // inversion: smallest k with CDF(k) > u
+        const double* cdf = p.cdf + Zr.cdf_off;
+        uint32_t lo = 0, hi = Zr.cdf_len - 1;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (cdf[mid] > u) hi = mid;
+          else lo = mid + 1;
+        }
+        cnt = (uint32_t)Zr.kmin + lo;
+        if (cnt) atomicAdd(&p.pending[(size_t)inst * p.R + Zr.rxn], (unsigned long long)cnt);
+      }
+    }
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<1024>(cnt, &s_total);
+    tot = s_total;
+    if (e < nz) p.zero_off[e] = carry + ex;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    p.zero_off[nz] = carry;
+    c->n_virtual = carry;
+    if (check_append && (uint64_t)c->n_slots + carry > p.capacity) atomicOr(&c->status, kStatCapacity);
+  }
+}
+
+template <bool kTable>
+__global__ void __launch_bounds__(256) k_count(KParams p) {
+  const DevCtrl* c = p.ctrl;
+  if (ctrl_status_warp(c)) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  const float4* __restrict__ st = cur_state(p, cur);
+  const uint32_t n_real = ld_u32(&c->n_slots), n_total = n_real + ld_u32(&c->n_virtual);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n_total; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    Out2 o;
+    o.n = 0;
+    if (i < n_real) advance_real<kTable, true>(p, st, i, o);
+    else if (i < n_total) advance_virtual(p, i - n_real, o);
+    warp_count(p.cell_count, o.n > 0 ? o.key[0] : kNoKey);
+    warp_count(p.cell_count, o.n > 1 ? o.key[1] : kNoKey);
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tiles(KParams p) {
+  __shared__ uint32_t s_total;
+  if (ld_u32(&p.ctrl->status)) return;
+  const uint32_t base = blockIdx.x * kScanTile;
+  uint32_t sum = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kScanTile / 1024; ++k) {
+    const uint32_t idx = base + k * 1024 + threadIdx.x;
+    if (idx < p.n_cells) sum += ld_u32(&p.cell_count[idx]);
+  }
+  block_exclusive_scan<1024>(sum, &s_total);
+  if (threadIdx.x == 0) p.tile_sums[blockIdx.x] = s_total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(KParams p) {
+  __shared__ uint32_t s_total;
+  DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < p.n_tiles; base += 1024) {
+    const uint32_t t = base + threadIdx.x;
+    const uint32_t v = t < p.n_tiles ? p.tile_sums[t] : 0u;
+    const uint32_t ex = block_exclusive_scan<1024>(v, &s_total);
+    const uint32_t tot = s_total;
+    if (t < p.n_tiles) p.tile_sums[t] = carry + ex;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    c->n_sorted = carry;
+    if (carry > p.capacity) atomicOr(&c->status, kStatCapacity);
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_down(KParams p) {
+  __shared__ uint32_t s_total;
+  DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;
+  constexpr uint32_t kPer = kScanTile / 1024;
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kPer;
+  uint32_t v[kPer];
+  uint32_t sum = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kPer; ++k) {
+    v[k] = (base + k < p.n_cells) ? ld_u32(&p.cell_count[base + k]) : 0u;
+    sum += v[k];
+  }
+  uint32_t run = p.tile_sums[blockIdx.x] + block_exclusive_scan<1024>(sum, &s_total);
+#pragma unroll
+  for (uint32_t k = 0; k < kPer; ++k) {
+    if (base + k < p.n_cells) p.cell_start[base + k] = run;
+    run += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) p.cell_start[p.n_cells] = ld_u32(&c->n_sorted);
+}
+
+template <bool kTable>
+__global__ void __launch_bounds__(256) k_scatter(KParams p) {
+  DevCtrl* c = p.ctrl;
+  if (ctrl_status_warp(c)) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  const float4* __restrict__ st = cur_state(p, cur);
+  const uint32_t n_real = ld_u32(&c->n_slots), n_total = n_real + ld_u32(&c->n_virtual);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n_total; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    Out2 o;
+    o.n = 0;
+    if (i < n_real) advance_real<kTable, false>(p, st, i, o);
+    else if (i < n_total) advance_virtual(p, i - n_real, o);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const uint32_t key = o.n > k ? o.key[k] : kNoKey;
+      const uint32_t off = warp_claim(p.cell_count, key);
+      if (key != kNoKey) {
+        const uint32_t slot = p.cell_start[key] + off;
+        if (slot < p.capacity) p.scatter[slot] = o.r[k];
+        else atomicOr(&c->status, kStatBounds);
+      }
+    }
+  }
+}
+
+// Position of record r among the records of its cell [s, e) in canonical
+// order; ties between identical records go by slot.
+__device__ __forceinline__ uint32_t canonical_rank(const float4* __restrict__ sc, uint32_t s, uint32_t e,
+                                                   uint32_t slot, const float4& r) {
+  uint32_t rank = 0;
+  for (uint32_t m = s; m < e; ++m) {
+    const float4 q = sc[m];
+    rank += (rec_less(q, r) || (m < slot && rec_equal(q, r))) ? 1u : 0u;
+  }
+  return rank;
+}
+
+__device__ __forceinline__ float dist2(const float4& a, const float4& b) {
+  const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+template <bool kHasBim>
+__global__ void __launch_bounds__(256) k_pairs(KParams p) {
+  DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  float4* __restrict__ nx = next_state(p, cur);
+  const float4* __restrict__ sc = p.scatter;
+  const uint32_t n = ld_u32(&c->n_sorted);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float4 r = sc[i];
+    const uint32_t w = rec_w(r);
+    const uint32_t inst = w >> 16, sp = w & 0xFFFFu;
+    const DevInstance& I = p.inst[inst];
+    const int cx = cell_coord(r.x, I.lo[0], I.inv[0], I.dims[0]);
+    const int cy = cell_coord(r.y, I.lo[1], I.inv[1], I.dims[1]);
+    const int cz = cell_coord(r.z, I.lo[2], I.inv[2], I.dims[2]);
+    const uint32_t key = I.cell_base + ((uint32_t)cz * I.dims[1] + (uint32_t)cy) * I.dims[0] + (uint32_t)cx;
+    const uint32_t s0 = p.cell_start[key], e0 = p.cell_start[key + 1];
+    if (i < s0 || i >= e0) {
+      atomicOr(&c->status, kStatBounds);
+      continue;
+    }
+    const uint32_t ci = s0 + canonical_rank(sc, s0, e0, i, r);
+    nx[ci] = r;
+    if (!kHasBim) continue;
+    if ((I.flags & (kInstFrozen | kInstRemoved)) || !(I.flags & kInstActive)) continue;
+    const DevSpecies S = p.species[I.block * p.S + sp];
+    if (S.max_r <= 0.0f) continue;
+
+    // distances to the six faces of the cell, for pruning neighbour cells
+    const float fx = __fsub_rn(__fmul_rn(__fsub_rn(r.x, I.lo[0]), I.inv[0]), (float)cx);
+    const float fy = __fsub_rn(__fmul_rn(__fsub_rn(r.y, I.lo[1]), I.inv[1]), (float)cy);
+    const float fz = __fsub_rn(__fmul_rn(__fsub_rn(r.z, I.lo[2]), I.inv[2]), (float)cz);
+    const float lox = fx * I.cell[0], hix = (1.0f - fx) * I.cell[0];
+    const float loy = fy * I.cell[1], hiy = (1.0f - fy) * I.cell[1];
+    const float loz = fz * I.cell[2], hiz = (1.0f - fz) * I.cell[2];
+    const float need = S.max_r + p.prune_margin * fminf(I.cell[0], fminf(I.cell[1], I.cell[2]));
+    const float need2 = need * need;
+    const uint32_t base_new = p.cell_start[I.cell_base];
+    const uint32_t t = p.inst_step[inst];
+    const int32_t* __restrict__ row = p.bim_table + sp * p.S;
+
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int nz_ = cz + dz;
+      if (nz_ < 0 || nz_ >= (int)I.dims[2]) continue;
+      const float ddz = dz < 0 ? loz : (dz > 0 ? hiz : 0.0f);
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int ny_ = cy + dy;
+        if (ny_ < 0 || ny_ >= (int)I.dims[1]) continue;
+        const float ddy = dy < 0 ? loy : (dy > 0 ? hiy : 0.0f);
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int nx_ = cx + dx;
+          if (nx_ < 0 || nx_ >= (int)I.dims[0]) continue;
+          const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
+          if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
+          const uint32_t nkey = I.cell_base + ((uint32_t)nz_ * I.dims[1] + (uint32_t)ny_) * I.dims[0] + (uint32_t)nx_;
+          const uint32_t ns = p.cell_start[nkey], ne = p.cell_start[nkey + 1];
+          for (uint32_t m = ns; m < ne; ++m) {
+            if (m == i) continue;
+            const float4 q = sc[m];
+            const int32_t b = row[rec_w(q) & 0xFFFFu];
+            if (b < 0) continue;
+            const DevBim& br = p.bim[I.block * p.B + (uint32_t)b];
+            if (dist2(r, q) > br.r2) continue;
+            const uint32_t cj = ns + canonical_rank(sc, ns, ne, m, q);
+            if (ci >= cj) continue;  // the pair is reported by its lower slot
+            if (br.prob < 1.0f) {
+              const U4 u = philox(U4{ci - base_new, t, kTagBimCoin, cj - base_new}, I.key_lo, I.key_hi);
+              if (!(u32_to_unit(u.x) < br.prob)) continue;
+            }
+            const uint32_t idx = atomicAdd(&c->n_pairs, 1u);
+            if (idx < p.pair_cap) {
+              p.pairs[idx] = DevPair{ci, cj, (uint32_t)b | (inst << 16), 0u};
+            } else {
+              atomicOr(&c->status, kStatPairs);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// Move the events of the committed step into the cumulative counters.
+__device__ __forceinline__ void commit_events(const KParams& p) {
+  const uint32_t n = p.n_inst * p.R;
+  for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const unsigned long long v = p.pending[e];
+    if (v) {
+      p.events[e] += v;
+      p.pending[e] = 0;
+    }
+  }
+}
+
+// Resolve the candidate pairs into a matching, apply the reactions and
+// commit the step.  Each particle reacts at most once; the pairs accepted
+// are those of the greedy scan in (lower slot, upper slot) order, found in
+// parallel as rounds of locally dominant pairs: a pair is taken when each
+// end's smallest undecided partner is the other end.
+__global__ void __launch_bounds__(1024) k_match(KParams p) {
+  __shared__ uint32_t s_more, s_deaths;
+  DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;
+  const uint32_t K = ld_u32(&c->n_pairs);
+  if (K > p.pair_cap) {
+    if (threadIdx.x == 0) atomicOr(&c->status, kStatPairs);
+    return;
+  }
+  const uint32_t cur = ld_u32(&c->cur);
+  float4* __restrict__ nx = next_state(p, cur);
+  DevPair* pr = p.pairs;
+  if (threadIdx.x == 0) s_deaths = 0;
+
+  for (uint32_t round = 0; round <= K; ++round) {
+    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+      if (pr[k].state == 0) {
+        atomicMin(&p.best[pr[k].i], pr[k].j);
+        atomicMin(&p.best[pr[k].j], pr[k].i);
+      }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+      if (pr[k].state == 0 && ld_u32(&p.best[pr[k].i]) == pr[k].j && ld_u32(&p.best[pr[k].j]) == pr[k].i)
+        pr[k].state = 3;
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+      if (pr[k].state == 3) {
+        atomicExch(&p.best[pr[k].i], kMatched);
+        atomicExch(&p.best[pr[k].j], kMatched);
+        pr[k].state = 1;
+      }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+      if (pr[k].state == 0 && (ld_u32(&p.best[pr[k].i]) == kMatched || ld_u32(&p.best[pr[k].j]) == kMatched))
+        pr[k].state = 2;
+    if (threadIdx.x == 0) s_more = 0;
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+      if (pr[k].state == 0) {
+        atomicExch(&p.best[pr[k].i], kFree);
+        atomicExch(&p.best[pr[k].j], kFree);
+        s_more = 1;
+      }
+    __syncthreads();
+    if (!s_more) break;
+  }
+
+  // products: at the D-weighted reaction point, displaced along a random
+  // direction when the reaction has an unbinding radius
+  for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+    const DevPair q = pr[k];
+    if (q.state != 1) continue;
+    const uint32_t inst = q.b >> 16, b = q.b & 0xFFFFu;
+    const DevInstance& I = p.inst[inst];
+    const DevBim br = p.bim[I.block * p.B + b];
+    const float4 ri = nx[q.i], rj = nx[q.j];
+    const bool i_first = (int32_t)(rec_w(ri) & 0xFFFFu) == br.react0;
+    const uint32_t m1 = i_first ? q.i : q.j, m2 = i_first ? q.j : q.i;
+    const float4 p1 = i_first ? ri : rj, p2 = i_first ? rj : ri;
+    const float rx = __fmaf_rn(br.x, p1.x, __fmul_rn(br.omx, p2.x));
+    const float ry = __fmaf_rn(br.x, p1.y, __fmul_rn(br.omx, p2.y));
+    const float rz = __fmaf_rn(br.x, p1.z, __fmul_rn(br.omx, p2.z));
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+    if (br.off0 != 0.0f || br.off1 != 0.0f) {
+      const uint32_t base_new = p.cell_start[I.cell_base];
+      unit_vector(q.i - base_new, p.inst_step[inst], kTagBimDir, q.j - base_new, I.key_lo, I.key_hi, dx, dy,
+                  dz);
+    }
+    uint32_t dead = 0;
+    float4 n1 = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kDead));
+    float4 n2 = n1;
+    if (br.prod0 >= 0) {
+      n1 = make_float4(reflect(__fmaf_rn(br.off0, dx, rx), I.lo[0], I.hi[0]),
+                       reflect(__fmaf_rn(br.off0, dy, ry), I.lo[1], I.hi[1]),
+                       reflect(__fmaf_rn(br.off0, dz, rz), I.lo[2], I.hi[2]),
+                       __uint_as_float(pack_w(inst, (uint32_t)br.prod0)));
+    } else {
+      ++dead;
+    }
+    if (br.prod1 >= 0) {
+      n2 = make_float4(reflect(__fmaf_rn(br.off1, dx, rx), I.lo[0], I.hi[0]),
+                       reflect(__fmaf_rn(br.off1, dy, ry), I.lo[1], I.hi[1]),
+                       reflect(__fmaf_rn(br.off1, dz, rz), I.lo[2], I.hi[2]),
+                       __uint_as_float(pack_w(inst, (uint32_t)br.prod1)));
+    } else {
+      ++dead;
+    }
+    nx[m1] = n1;
+    nx[m2] = n2;
+    atomicAdd(&p.pending[(size_t)inst * p.R + br.rxn], 1ull);
+    if (dead) atomicAdd(&s_deaths, dead);
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+    atomicExch(&p.best[pr[k].i], kFree);
+    atomicExch(&p.best[pr[k].j], kFree);
+  }
+  commit_events(p);
+  for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) {
+    const DevInstance& I = p.inst[inst];
+    if ((I.flags & kInstActive) && !(I.flags & (kInstFrozen | kInstRemoved))) p.inst_step[inst] += 1;
+    p.inst_slot_base[inst] = p.cell_start[I.cell_base];
+  }
+  if (threadIdx.x == 0) {
+    c->n_pairs_last = K;
+    c->n_pairs = 0;
+    c->deaths_last = s_deaths;
+    c->n_slots = c->n_sorted;
+    c->n_virtual = 0;
+    c->cur = cur ^ 1u;
+    c->step += 1;
+    c->steps_done += 1;
+  }
+}
+
+template <bool kTable>
+__global__ void __launch_bounds__(256) k_diffuse(KParams p) {
+  const DevCtrl* c = p.ctrl;
+  if (ctrl_status_warp(c)) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  float4* st = cur ? p.state[1] : p.state[0];
+  const uint32_t n = ld_u32(&c->n_slots);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    Out2 o;
+    advance_real<kTable, false>(p, st, i, o);
+    if (o.n > 0) st[i] = o.r[0];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_append(KParams p) {
+  const DevCtrl* c = p.ctrl;
+  if (ctrl_status_warp(c)) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  float4* st = cur ? p.state[1] : p.state[0];
+  const uint32_t n = ld_u32(&c->n_slots), nv = ld_u32(&c->n_virtual);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += stride) {
+    Out2 o;
+    advance_virtual(p, v, o);
+    st[n + v] = o.r[0];
+  }
+}
+
+__global__ void k_finalize_inplace(KParams p) {
+  DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;
+  commit_events(p);
+  for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) {
+    const DevInstance& I = p.inst[inst];
+    if ((I.flags & kInstActive) && !(I.flags & (kInstFrozen | kInstRemoved))) p.inst_step[inst] += 1;
+  }
+  if (threadIdx.x == 0) {
+    c->n_slots += c->n_virtual;
+    c->n_virtual = 0;
+    c->n_pairs_last = 0;
+    c->deaths_last = 0;
+    c->step += 1;
+    c->steps_done += 1;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_instance_counts(KParams p, unsigned long long* counts) {
+  const DevCtrl* c = p.ctrl;
+  const uint32_t cur = ld_u32(&c->cur);
+  const float4* st = cur_state(p, cur);
+  const uint32_t n = ld_u32(&c->n_slots);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t key = kNoKey;
+    if (i < n) {
+      const uint32_t w = rec_w(st[i]);
+      if (w != kDead) key = w >> 16;
+    }
+    const uint32_t peers = __match_any_sync(kFull, key);
+    if (key != kNoKey && lane_id() == (uint32_t)(__ffs(peers) - 1))
+      atomicAdd(&counts[key], (unsigned long long)__popc(peers));
+  }
+}
+
+}  // namespace
+
+void enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
+                  const LaunchShape& shape, cudaStream_t s) {
+  (void)has_uni;
+  const int gs = shape.grid_stream, bs = shape.block_stream;
+  if (has_zero) k_zeroth<<<1, 1024, 0, s>>>(p, path == Path::kDiffuseOnly ? 1 : 0);
+  if (path == Path::kDiffuseOnly) {
+    if (table) k_diffuse<true><<<gs, bs, 0, s>>>(p);
+    else k_diffuse<false><<<gs, bs, 0, s>>>(p);
+    if (has_zero) k_append<<<gs, bs, 0, s>>>(p);
+    k_finalize_inplace<<<1, 256, 0, s>>>(p);
+    return;
+  }
+  if (table) k_count<true><<<gs, bs, 0, s>>>(p);
+  else k_count<false><<<gs, bs, 0, s>>>(p);
+  k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
+  k_scan_top<<<1, 1024, 0, s>>>(p);
+  k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
+  if (table) k_scatter<true><<<gs, bs, 0, s>>>(p);
+  else k_scatter<false><<<gs, bs, 0, s>>>(p);
+  if (has_bim) k_pairs<true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+  else k_pairs<false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+  k_match<<<1, 1024, 0, s>>>(p);
+}
+
+void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaStream_t s) {
+  k_instance_counts<<<152 * 4, 256, 0, s>>>(p, counts);
+}
+
+}  // namespace bd

@@ -1,0 +1,57 @@
+// bd_kernels.h -- launch interface of the step kernels (host side).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bd_layout.h"
+
+namespace bd {
+
+// Everything a step kernel reads or writes, passed by value.
+struct KParams {
+  float4* state[2];           // ping-pong state buffers, DevCtrl::cur selects
+  float4* scatter;            // cell-ordered staging buffer of the sort
+  DevCtrl* ctrl;
+  const DevInstance* inst;
+  const DevSpecies* species;  // [block][S]
+  const DevUni* uni;          // [block][U]
+  const DevBim* bim;          // [block][B]
+  const DevZero* zero;        // [block][Z]
+  const double* cdf;          // Poisson CDFs (absolute offsets in DevZero)
+  const int32_t* bim_table;   // [S][S] -> local second-order index or -1
+  const float* gauss;         // 4096 N(0,1) quantiles (table mode)
+  uint32_t* inst_step;        // [I] steps taken by each instance
+  uint32_t* inst_slot_base;   // [I] first slot of each instance in the current state
+  uint32_t* zero_off;         // [I*Z + 1] prefix of zeroth-order births
+  uint32_t* cell_count;       // [n_cells] particles per cell (returns to 0 each step)
+  uint32_t* cell_start;       // [n_cells + 1] exclusive prefix of cell_count
+  uint32_t* tile_sums;        // [n_tiles] scan partials
+  DevPair* pairs;             // [pair_cap]
+  uint32_t* best;             // [capacity] matcher scratch, all 0xFFFFFFFF between steps
+  unsigned long long* events; // [I * R] reaction event counters (committed steps)
+  unsigned long long* pending;// [I * R] events of the step in flight, added at commit
+  uint32_t n_inst, S, U, B, Z, R;
+  uint32_t n_cells, n_tiles;
+  uint32_t capacity, pair_cap;
+  float prune_margin;         // fraction of a cell edge added to pruning distances
+};
+
+enum class Path { kDiffuseOnly, kSorted };
+
+struct LaunchShape {
+  int grid_stream;            // blocks of the grid-stride particle kernels
+  int block_stream;           // threads per block of those kernels
+  int grid_pairs, block_pairs;
+};
+
+// Enqueue one full step on `stream`.  table selects the normal generator.
+void enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
+                  const LaunchShape& shape, cudaStream_t stream);
+
+// Count live records per instance (counts[I] must be zeroed).
+void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaStream_t stream);
+
+// Tile size of the cell scan.
+constexpr uint32_t kScanTile = 4096;
+
+}  // namespace bd

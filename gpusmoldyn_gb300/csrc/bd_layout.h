@@ -1,0 +1,119 @@
+// bd_layout.h -- device-side data layout of one simulation handle, shared by
+// the host packer (bd_api.cpp) and the kernels (bd_kernels.cu).
+//
+// Particle record: one float4 per slot, x, y, z and a 32-bit word w holding
+// species (bits 0-15) and instance (bits 16-31); w = 0xFFFFFFFF marks an empty
+// slot (a particle that died in the bimolecular phase).  The reference keeps
+// positions (float4, w = radius/flag) and types (int) in two arrays
+// (particleSystem.h:151-152, 204-205); one 16-byte record halves the number
+// of memory transactions per particle.
+//
+// Parameters live in "blocks": one block per ensemble instance (a single
+// system has one).  Every block has the same shape (species S, first-order
+// reactions U, second-order reactions B, zeroth-order reactions Z) because
+// the instances of an ensemble share one reaction network and differ only in
+// numbers.  The second-order lookup table (S x S -> local reaction index) is
+// shared by all blocks, like the reference's reactionTable
+// (particleSystem.cpp:653-673).
+#pragma once
+#include <stdint.h>
+
+namespace bd {
+
+constexpr uint32_t kDead = 0xFFFFFFFFu;
+constexpr uint32_t kMaxSpecies = 0xFFFEu;
+constexpr uint32_t kMaxInstances = 0xFFFFu;
+
+// Philox counter word 2 carries a stream tag in its top byte.
+enum StreamTag : uint32_t {
+  kTagDiffuse = 1u << 24,   // 3 normals per particle per step
+  kTagUniCoin = 2u << 24,   // first-order coins, 4 per counter (low bits = k/4)
+  kTagUniDir = 3u << 24,    // product direction of a first-order birth
+  kTagZeroCount = 4u << 24, // Poisson count of one zeroth-order reaction
+  kTagZeroPos = 5u << 24,   // position of one zeroth-order birth
+  kTagBimCoin = 6u << 24,   // coin of one candidate pair
+  kTagBimDir = 7u << 24,    // product direction of one accepted pair
+};
+
+struct DevSpecies {        // 16 B
+  float sigma;             // rms step per axis, sqrt(2 D dt) (molSetTimestep)
+  float max_r;             // largest binding radius over this species' pairs (0 = inert)
+  uint32_t uni_begin;      // first-order reactions of this species: [begin, begin+count)
+  uint32_t uni_count;      // in the block's DevUni array (reactionOrderInfo[1] CSR)
+};
+
+struct DevUni {            // 32 B
+  float prob;              // conditional per-step probability (rxnsetrate order 1)
+  int32_t prod0, prod1;    // product species, -1 = none (prod0 < 0: decay)
+  float off0, off1;        // product displacements along a random unit vector
+  uint32_t rxn;            // global reaction index (event counters)
+  uint32_t pad[2];
+};
+
+struct DevBim {            // 48 B
+  float r2;                // squared binding radius
+  float prob;              // reaction probability once within r2 (1 = always)
+  float x, omx;            // reaction point x*p1 + omx*p2 (p1 = first reactant)
+  int32_t react0;          // species of the first reactant
+  int32_t prod0, prod1;    // product species, -1 = none
+  float off0, off1;        // product displacements along a random unit vector
+  uint32_t rxn;            // global reaction index
+  uint32_t pad[2];
+};
+
+struct DevZero {           // 32 B
+  int32_t prod0, prod1;    // product species (prod1 = -1 for one product)
+  uint32_t cdf_off;        // offset of the Poisson CDF in the block's CDF array
+  uint32_t cdf_len;        // entries: P(X <= kmin + k), k = 0..len-1
+  int32_t kmin;
+  uint32_t rxn;            // global reaction index
+  uint32_t pad[2];
+};
+
+enum InstanceFlags : uint32_t {
+  kInstActive = 1u,        // advanced every step
+  kInstFrozen = 2u,        // kept in place, not advanced (finished request)
+  kInstRemoved = 4u,       // dropped at the next sort
+};
+
+struct DevInstance {       // 80 B
+  float lo[3], hi[3];      // reflecting box
+  float inv[3];            // cells per unit length per axis
+  float cell[3];           // cell edge per axis
+  uint32_t dims[3];        // cells per axis
+  uint32_t cell_base;      // first global cell key of this instance
+  uint32_t key_lo, key_hi; // Philox key (instance seed)
+  uint32_t block;          // parameter block
+  uint32_t flags;          // InstanceFlags
+};
+
+// Mutable per-step control words, one per handle, in device memory.
+struct DevCtrl {
+  uint32_t cur;            // state buffer holding the current step (0/1)
+  uint32_t n_slots;        // slots of the current state (holes included)
+  uint32_t n_virtual;      // zeroth-order births of the step in flight
+  uint32_t n_sorted;       // slots of the next state
+  uint32_t n_pairs;        // candidate pairs appended by the pair kernel
+  uint32_t n_pairs_last;   // candidate pairs of the last completed step
+  uint32_t status;         // StatusBits, 0 = healthy
+  uint32_t steps_done;     // completed steps since the last host reset
+  uint64_t step;           // global step counter
+  uint32_t deaths_last;    // bimolecular deaths of the last step
+  uint32_t pad[5];
+};
+
+enum StatusBits : uint32_t {
+  kStatCapacity = 1u,      // next state would exceed the slot capacity
+  kStatPairs = 2u,         // candidate pairs exceed the pair capacity
+  kStatBounds = 4u,        // a device-side bounds check failed
+  kStatTimeout = 8u,       // a bounded wait ran out
+};
+
+// Pair list entry written by the pair kernel and resolved by the matcher.
+struct DevPair {           // 16 B
+  uint32_t i, j;           // canonical slots, i < j
+  uint32_t b;              // local second-order reaction index | instance << 16
+  uint32_t state;          // 0 undecided, 1 accepted, 2 rejected
+};
+
+}  // namespace bd

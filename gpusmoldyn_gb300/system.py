@@ -1,0 +1,244 @@
+"""Pythonic handle over the C ABI: one simulation or one batched ensemble."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class System:
+    """One Brownian-dynamics simulation (or ensemble) resident on one GPU.
+
+    ``instances`` (list of dicts with box_lo, box_hi, seed, d_scale, k2_scale,
+    cell_size) makes an ensemble of independent instances sharing the
+    species and reaction network."""
+
+    def __init__(self, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), dt=1e-3, seed=1, normals="boxmuller",
+                 capacity=0, cell_size=0.0, cell_occupancy=0.0, pair_capacity=0, device=0, instances=None):
+        self.lib = L.load()
+        cfg = L.bd_config()
+        self.lib.bd_config_default(C.byref(cfg))
+        for a in range(3):
+            cfg.box_lo[a] = box_lo[a]
+            cfg.box_hi[a] = box_hi[a]
+        cfg.dt = dt
+        cfg.seed = seed
+        cfg.capacity = int(capacity)
+        cfg.cell_size = cell_size
+        cfg.cell_occupancy = cell_occupancy
+        cfg.pair_capacity = int(pair_capacity)
+        cfg.device = device
+        cfg.normal_mode = L.BD_NORMALS_TABLE if normals == "table" else L.BD_NORMALS_BOXMULLER
+        self.cfg = cfg
+        self.dt = dt
+        self.h = C.c_void_p()
+        if instances is None:
+            L.check(self.lib.bd_create(C.byref(cfg), C.byref(self.h)), "bd_create")
+            self.n_instances = 1
+            self.instances = [dict(box_lo=tuple(box_lo), box_hi=tuple(box_hi), seed=seed, d_scale=1.0,
+                                   k2_scale=1.0, cell_size=0.0)]
+        else:
+            arr = (L.bd_instance_desc * len(instances))()
+            for k, d in enumerate(instances):
+                for a in range(3):
+                    arr[k].box_lo[a] = d["box_lo"][a]
+                    arr[k].box_hi[a] = d["box_hi"][a]
+                arr[k].seed = d.get("seed", k + 1)
+                arr[k].d_scale = d.get("d_scale", 1.0)
+                arr[k].k2_scale = d.get("k2_scale", 1.0)
+                arr[k].cell_size = d.get("cell_size", 0.0)
+            L.check(self.lib.bd_create_ensemble(C.byref(cfg), arr, len(instances), C.byref(self.h)),
+                    "bd_create_ensemble")
+            self.n_instances = len(instances)
+            self.instances = [dict(d) for d in instances]
+        self.n_species = 0
+        self.n_reactions = 0
+
+    # ------------------------------------------------------------- set-up
+    def add_species(self, D: float) -> int:
+        i = C.c_int()
+        L.check(self.lib.bd_add_species(self.h, D, C.byref(i)), "bd_add_species")
+        self.n_species += 1
+        return i.value
+
+    def add_reaction(self, order, reactants=(), products=(), rate=0.0) -> int:
+        r = (C.c_int * 2)(*(list(reactants) + [-1, -1])[:2])
+        p = (C.c_int * 2)(*(list(products) + [-1, -1])[:2])
+        i = C.c_int()
+        L.check(self.lib.bd_add_reaction(self.h, order, r, p, rate, C.byref(i)), "bd_add_reaction")
+        self.n_reactions += 1
+        return i.value
+
+    def set_product_placement(self, rxn, kind, param=0.0):
+        L.check(self.lib.bd_set_product_placement(self.h, rxn, kind, param), "bd_set_product_placement")
+
+    def set_reaction_probability(self, rxn, prob):
+        L.check(self.lib.bd_set_reaction_probability(self.h, rxn, prob), "bd_set_reaction_probability")
+
+    def finalize(self, allow=(L.BD_OK, L.BD_ERR_PGEM_UNATTAINABLE)):
+        st = self.lib.bd_finalize(self.h)
+        L.check(st, "bd_finalize", ok=allow)
+        return st
+
+    def reaction_info(self, rxn, instance=0) -> dict:
+        ri = L.bd_reaction_info()
+        L.check(self.lib.bd_get_instance_reaction_info(self.h, instance, rxn, C.byref(ri)), "reaction_info")
+        return dict(order=ri.order, nprod=ri.nprod, reactants=list(ri.reactants), products=list(ri.products),
+                    rate=ri.rate, prob=ri.prob, bind_radius=ri.bind_radius, unbind_radius=ri.unbind_radius,
+                    geminate_prob=ri.geminate_prob, product_offsets=list(ri.product_offsets),
+                    reverse=ri.reverse, flags=ri.flags)
+
+    def species_d(self, instance=0) -> np.ndarray:
+        out = np.zeros(self.n_species, np.float32)
+        for s in range(self.n_species):
+            v = C.c_float()
+            L.check(self.lib.bd_get_species_d(self.h, instance, s, C.byref(v)), "species_d")
+            out[s] = v.value
+        return out
+
+    def poisson_cdf(self, rxn, instance=0):
+        kmin = C.c_int()
+        n = C.c_size_t()
+        L.check(self.lib.bd_get_poisson_cdf(self.h, instance, rxn, None, 0, C.byref(kmin), C.byref(n)), "cdf")
+        buf = np.zeros(n.value, np.float64)
+        L.check(self.lib.bd_get_poisson_cdf(self.h, instance, rxn, _ptr(buf), n.value, C.byref(kmin),
+                                            C.byref(n)), "cdf")
+        return buf, kmin.value
+
+    # ---------------------------------------------------------- particles
+    def set_particles(self, pos, species):
+        pos = np.asarray(pos, np.float32)
+        n = pos.shape[0]
+        p4 = np.zeros((n, 4), np.float32)
+        p4[:, :3] = pos[:, :3]
+        sp = np.ascontiguousarray(species, np.int32)
+        L.check(self.lib.bd_set_particles(self.h, _ptr(p4), _ptr(sp), n), "bd_set_particles")
+
+    def set_ensemble_particles(self, pos, species, counts):
+        pos = np.asarray(pos, np.float32)
+        n = pos.shape[0]
+        p4 = np.zeros((n, 4), np.float32)
+        p4[:, :3] = pos[:, :3]
+        sp = np.ascontiguousarray(species, np.int32)
+        cnt = np.ascontiguousarray(counts, np.uint64)
+        L.check(self.lib.bd_set_ensemble_particles(self.h, _ptr(p4), _ptr(sp), _ptr(cnt), len(cnt)),
+                "bd_set_ensemble_particles")
+
+    def step(self, n=1):
+        L.check(self.lib.bd_step(self.h, int(n)), "bd_step")
+
+    def synchronize(self, allow_empty=True):
+        st = self.lib.bd_synchronize(self.h)
+        L.check(st, "bd_synchronize", ok=(L.BD_OK, L.BD_ERR_EMPTY) if allow_empty else (L.BD_OK,))
+        return st
+
+    def count(self) -> int:
+        v = C.c_uint64()
+        L.check(self.lib.bd_get_count(self.h, C.byref(v)), "bd_get_count")
+        return v.value
+
+    def step_count(self) -> int:
+        v = C.c_uint64()
+        L.check(self.lib.bd_get_step(self.h, C.byref(v)), "bd_get_step")
+        return v.value
+
+    def particles(self, instance=-1):
+        n = self.count() if instance < 0 else int(self.instance_counts()[instance])
+        pos = np.zeros((max(n, 1), 4), np.float32)
+        sp = np.zeros(max(n, 1), np.int32)
+        got = C.c_size_t()
+        L.check(self.lib.bd_get_instance_particles(self.h, instance, _ptr(pos), _ptr(sp), n, C.byref(got)),
+                "bd_get_particles")
+        m = min(got.value, n)
+        return pos[:m, :3].copy(), sp[:m].copy()
+
+    def instance_counts(self) -> np.ndarray:
+        out = np.zeros(self.n_instances, np.uint64)
+        L.check(self.lib.bd_get_instance_counts(self.h, _ptr(out), self.n_instances), "instance_counts")
+        return out
+
+    def slots(self):
+        n = C.c_size_t()
+        L.check(self.lib.bd_debug_get_slots(self.h, None, None, 0, C.byref(n)), "slots")
+        xyz = np.zeros((max(n.value, 1), 4), np.float32)
+        w = np.zeros(max(n.value, 1), np.uint32)
+        L.check(self.lib.bd_debug_get_slots(self.h, _ptr(xyz), _ptr(w), n.value, C.byref(n)), "slots")
+        return xyz[:n.value, :3].copy(), w[:n.value].copy()
+
+    def cells(self) -> np.ndarray:
+        n = C.c_size_t()
+        L.check(self.lib.bd_debug_get_cells(self.h, None, 0, C.byref(n)), "cells")
+        out = np.zeros(n.value + 1, np.uint32)
+        L.check(self.lib.bd_debug_get_cells(self.h, _ptr(out), n.value + 1, C.byref(n)), "cells")
+        return out
+
+    def pairs(self) -> np.ndarray:
+        n = C.c_size_t()
+        L.check(self.lib.bd_debug_get_pairs(self.h, None, 0, C.byref(n)), "pairs")
+        out = np.zeros((max(n.value, 1), 4), np.uint32)
+        L.check(self.lib.bd_debug_get_pairs(self.h, _ptr(out), n.value, C.byref(n)), "pairs")
+        return out[:n.value].copy()
+
+    def grid(self, instance=0):
+        dims = np.zeros(3, np.uint32)
+        cell = np.zeros(3, np.float32)
+        inv = np.zeros(3, np.float32)
+        L.check(self.lib.bd_get_grid(self.h, instance, _ptr(dims), _ptr(cell), _ptr(inv)), "bd_get_grid")
+        return dims, cell, inv
+
+    def event_counts(self) -> np.ndarray:
+        out = np.zeros(max(self.n_reactions, 1), np.uint64)
+        L.check(self.lib.bd_get_event_counts(self.h, _ptr(out), self.n_reactions), "event_counts")
+        return out[:self.n_reactions]
+
+    def state_pointer(self):
+        p = C.c_void_p()
+        n = C.c_uint64()
+        L.check(self.lib.bd_get_state_pointer(self.h, C.byref(p), C.byref(n)), "state_pointer")
+        return p.value, n.value
+
+    def close(self):
+        if self.h:
+            self.lib.bd_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def gauss_table(n=4096) -> np.ndarray:
+    lib = L.load()
+    out = np.zeros(n, np.float32)
+    lib.bd_gauss_table(_ptr(out), n)
+    return out
+
+
+def numrxnrate(step, a, b):
+    return L.load().bd_numrxnrate(step, a, b)
+
+
+def actrxnrate(step, a):
+    return L.load().bd_actrxnrate(step, a)
+
+
+def bindingradius(rate, dt, difc, b, rel=0):
+    return L.load().bd_bindingradius(rate, dt, difc, b, rel)
+
+
+def unbindingradius(pgem, dt, difc, a):
+    return L.load().bd_unbindingradius(pgem, dt, difc, a)

@@ -1,0 +1,270 @@
+/*
+ * gpusmoldyn.h -- C ABI of the GB300 Brownian-dynamics step (libgpusmoldyn.so).
+ *
+ * One handle owns one simulation (or a batched ensemble of independent
+ * instances) resident on one GPU: species with per-species diffusion
+ * coefficients, zeroth-, first- and second-order reactions whose probabilities
+ * and binding / unbinding radii are derived with the Andrews-Bray rxnparam
+ * method, reflecting walls in a rectangular box, and a per-timestep pipeline
+ * of hand-written sm_103a kernels.  All entry points take plain pointers and
+ * sizes and return a bd_status (0 = success); none aborts the process.
+ *
+ * This ABI replaces the reference's extern "C" CUDA layer
+ * (particleSystem.cuh:29-110) and the device-facing part of its
+ * ParticleSystem class (particleSystem.h:50-218); each declaration below
+ * names the reference function(s) it stands in for.  Handles are independent:
+ * there is no file-scope device state (the reference keeps SimParams, the
+ * Gaussian table and textures in file-static device symbols,
+ * particles_kernel.cu:42-57), so several handles may live in one process.
+ */
+#ifndef GPUSMOLDYN_H
+#define GPUSMOLDYN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define BD_EXTERN extern "C"
+#else
+#define BD_EXTERN
+#endif
+#define BD_API BD_EXTERN __attribute__((visibility("default")))
+
+/* ------------------------------------------------------------------ status */
+/* The setup codes 1, 2, 4, 7 and 8 keep the numbers the reference's
+ * rxnsetrate / rxnsetproduct return (smolreact.cpp:274-282, 455-469). */
+typedef int bd_status;
+enum {
+  BD_OK = 0,
+  BD_ERR_NEGATIVE_RATE = 1,        /* rate < 0 (rxnsetrate return 1) */
+  BD_ERR_STATE_DEPENDENT = 2,      /* reserved: per-state probabilities (return 2) */
+  BD_ERR_ZERO_DIFFUSION = 4,       /* both reactants (or products) have D = 0 */
+  BD_ERR_ILLEGAL_UNBIND = 7,       /* unbinding radius from illegal input (er = 7) */
+  BD_ERR_PGEM_UNATTAINABLE = 8,    /* requested geminate probability too high (er = 8) */
+  BD_ERR_INVALID_ARGUMENT = 16,
+  BD_ERR_NOT_FINALIZED = 17,       /* step/particles before bd_finalize */
+  BD_ERR_ALREADY_FINALIZED = 18,   /* species/reactions after bd_finalize */
+  BD_ERR_CAPACITY = 19,            /* particle or pair capacity exceeded, no room to grow */
+  BD_ERR_EMPTY = 20,               /* no particles left: reference update() returns false */
+  BD_ERR_CUDA = 21,                /* a CUDA runtime call failed */
+  BD_ERR_TIMEOUT = 22,             /* a bounded device-side wait ran out */
+  BD_ERR_NO_DEVICE = 23,
+  BD_ERR_DEVICE_STATE = 24,        /* device reported an inconsistent state (bounds check) */
+  BD_ERR_UNSUPPORTED = 25
+};
+
+/* ------------------------------------------------------------------ types */
+typedef struct bd_system *bd_handle;
+
+enum { BD_NORMALS_BOXMULLER = 0, BD_NORMALS_TABLE = 1 };
+
+/* bd_config.device value for a host-only handle: set-up, parameter
+ * derivation, grid planning and the getters work without a GPU; stepping
+ * returns BD_ERR_NO_DEVICE. */
+#define BD_DEVICE_NONE (-1)
+
+/* Product-placement kinds for reactions with two products (Smoldyn's rparam
+ * types; the reference hard-codes pgem = 0.2, smolreact.cpp:373-376). */
+enum {
+  BD_PP_DEFAULT = 0,     /* irreversible: products at the reaction point;
+                            reversible pair: PGEMMAX 0.2 (Smoldyn's default) */
+  BD_PP_PGEM = 1,        /* param = geminate probability; error 8 if unattainable */
+  BD_PP_PGEMMAX = 2,     /* param = max geminate probability; b = 0 if the
+                            attainable maximum is below it */
+  BD_PP_UNBINDRAD = 3,   /* param = unbinding radius b (length) */
+  BD_PP_OFFSET0 = 4      /* products exactly at the reaction point (b = 0) */
+};
+
+typedef struct bd_config {
+  float box_lo[3];           /* reflecting box, replaces the fixed [-1,1]^3 world */
+  float box_hi[3];           /* (particleSystem.cpp:73, particleSystem.h:114-120) */
+  float dt;                  /* time step (particleSystem.h:147 deltaTime) */
+  uint64_t seed;             /* Philox key; replaces srand(time(0)) MT seeding */
+  uint64_t capacity;         /* particle slots; 0 = 2x the first particle upload */
+  float cell_size;           /* uniform-grid cell edge; 0 = automatic */
+  float cell_occupancy;      /* target particles per cell for automatic sizing (0 = 3) */
+  int normal_mode;           /* BD_NORMALS_* */
+  int device;                /* CUDA device ordinal */
+  uint32_t pair_capacity;    /* candidate-pair list length; 0 = automatic */
+  uint32_t reserved[7];
+} bd_config;
+
+/* Derived parameters of one reaction, as the reference stores them in its
+ * struct-of-arrays Reaction (reaction.h:36-48). */
+typedef struct bd_reaction_info {
+  int order, nprod;
+  int reactants[2], products[2];
+  float rate;                 /* as given */
+  float prob;                 /* per-step probability (order 0: Poisson mean) */
+  float bind_radius;          /* order 2: a */
+  float unbind_radius;        /* b for the products of this reaction (0 if none) */
+  float geminate_prob;        /* the pgem actually achieved (order 1 reverse) */
+  float product_offsets[2];   /* signed displacement of each product along a
+                                 random unit vector (rxnsetproduct x offsets) */
+  int reverse;                /* index of the reverse reaction, -1 if none */
+  int flags;                  /* bit 0: pgem fell back to b = 0 */
+} bd_reaction_info;
+
+/* ----------------------------------------------------- lifetime & set-up */
+
+/* Fill a config with defaults (unit box, dt = 1e-3, seed 1). */
+BD_API void bd_config_default(bd_config *cfg);
+
+/* Create a simulation on cfg->device.  Replaces ParticleSystem::ParticleSystem
+ * + _initialize (particleSystem.cpp:49-88, 573-751), cudaInit
+ * (particleSystemCuda.cu:46-54) and initializeMT (:139-145). */
+BD_API bd_status bd_create(const bd_config *cfg, bd_handle *out);
+
+/* Free every host and device allocation.  Replaces ~ParticleSystem /
+ * _finalize (particleSystem.cpp:90-94, 753-826) and freeArray (:72-75). */
+BD_API bd_status bd_destroy(bd_handle h);
+
+/* Add a species with diffusion coefficient D; *id receives its index.
+ * Replaces the hard-coded test*Types presets (particleSystem.cpp:381-571)
+ * and molSetTimestep (:137-142). */
+BD_API bd_status bd_add_species(bd_handle h, float D, int *id);
+
+/* Add a reaction of order 0, 1 or 2; unused reactant/product slots are -1.
+ * Replaces the test*Reactions presets (particleSystem.cpp:319-542). */
+BD_API bd_status bd_add_reaction(bd_handle h, int order, const int reactants[2],
+                                 const int products[2], float rate, int *id);
+
+/* Per-encounter probability of a second-order reaction (Smoldyn's reaction
+ * probability; the reference keeps Reaction::prob = 1, smolreact.cpp:382-383,
+ * and draws a coin only when it is below 1, particles_kernel.cu:395-396). */
+BD_API bd_status bd_set_reaction_probability(bd_handle h, int rxn, float prob);
+
+/* Choose how the two products of reaction rxn are placed (BD_PP_*). */
+BD_API bd_status bd_set_product_placement(bd_handle h, int rxn, int kind, float param);
+
+/* Derive probabilities, binding and unbinding radii and product offsets and
+ * upload the reaction tables.  Replaces fillReactionOrderInfo, rxnsetrate,
+ * rxnsetproduct (smolreact.cpp:173-483), the reaction-table fill and upload
+ * (particleSystem.cpp:635-700), createGaussTable + copyGaussianToConstant
+ * (stats.cpp:277-282, particleSystemCuda.cu:134-137) and setParameters
+ * (:121-125).  Returns the first setup error code; a pgem fallback to b = 0
+ * is not an error (see bd_reaction_info.flags). */
+BD_API bd_status bd_finalize(bd_handle h);
+
+BD_API bd_status bd_get_reaction_info(bd_handle h, int rxn, bd_reaction_info *out);
+BD_API bd_status bd_get_counts(bd_handle h, int *n_species, int *n_reactions);
+
+/* ------------------------------------------------------------ particles */
+
+/* Upload n particles from host memory: xyz4 holds x,y,z,(ignored) per
+ * particle, species[i] the species id.  Replaces reset / setArray
+ * (particleSystem.cpp:1057-1161, which never upload in headless mode) and
+ * copyArrayToDevice (particleSystemCuda.cu:93-96). */
+BD_API bd_status bd_set_particles(bd_handle h, const float *xyz4, const int *species, size_t n);
+
+/* Live particle count (synchronises).  Replaces getNumParticles
+ * (particleSystem.h:86) and the per-step count readbacks of
+ * compactPosAndType (particleSystemCuda.cu:298-306). */
+BD_API bd_status bd_get_count(bd_handle h, uint64_t *n);
+
+/* Copy live particles to host memory (synchronises): up to cap particles,
+ * *n receives the live count.  Replaces getArray / copyArrayFromDevice
+ * (particleSystem.cpp:1031-1055, particleSystemCuda.cu:82-91). */
+BD_API bd_status bd_get_particles(bd_handle h, float *xyz4, int *species, size_t cap, size_t *n);
+
+/* Device address of the current record array (float4 x, y, z, w where w's
+ * bits hold species | instance << 16, 0xFFFFFFFF = empty slot) and its slot
+ * count, after synchronising; valid until the next bd_step.  Replaces
+ * getCudaPosVBO / getCudaTypesVBO (particleSystem.h:94-95). */
+BD_API bd_status bd_get_state_pointer(bd_handle h, void **dev_records, uint64_t *n_slots);
+
+/* ----------------------------------------------------------------- step */
+
+/* Enqueue nsteps timesteps on the handle's stream without host
+ * synchronisation.  Replaces ParticleSystem::update (particleSystem.cpp:
+ * 829-1001) and through it integrateSystem, adjustPositions, calcHash,
+ * RadixSort::sort, reorderDataAndFindCellStart, collide and
+ * compactPosAndType (particleSystemCuda.cu:148-367) and zeroReact
+ * (reaction_cpu.cpp:36-63). */
+BD_API bd_status bd_step(bd_handle h, int nsteps);
+
+/* Wait for enqueued steps; if a step ran out of particle or pair capacity
+ * the buffers grow and the remaining steps are replayed, so the state after
+ * return is the state after every requested step.  Returns BD_ERR_EMPTY when
+ * no particle is left (update() returning false, particleSystem.cpp:892,963).
+ * Replaces threadSync (particleSystemCuda.cu:77-80). */
+BD_API bd_status bd_synchronize(bd_handle h);
+
+/* Completed steps. */
+BD_API bd_status bd_get_step(bd_handle h, uint64_t *step);
+
+/* Cumulative event count per reaction (n entries). */
+BD_API bd_status bd_get_event_counts(bd_handle h, uint64_t *counts, int n);
+
+/* Per-step kernel time breakdown of the last bd_step batch, in ms
+ * (diagnostics; zeros unless BD_TIMING=1 in the environment). */
+BD_API bd_status bd_get_stage_times(bd_handle h, float *ms, int n);
+
+/* --------------------------------------------------- parity / inspection */
+
+/* Raw slot array of the current state, holes included (w = 0xFFFFFFFF). */
+BD_API bd_status bd_debug_get_slots(bd_handle h, float *xyz4, uint32_t *w, size_t cap, size_t *n);
+/* Cell start offsets of the last sorted step (ncells + 1 entries). */
+BD_API bd_status bd_debug_get_cells(bd_handle h, uint32_t *start, size_t cap, size_t *ncells);
+/* Candidate pairs (slot_i, slot_j, reaction, accepted) of the last step. */
+BD_API bd_status bd_debug_get_pairs(bd_handle h, uint32_t *quads, size_t cap, size_t *n);
+/* Uniform-grid geometry of one instance: cells per axis, cell edge lengths
+ * and cells per unit length (the float factors the cell key is computed
+ * with).  Replaces getGridSize / getCellSize / getWorldOrigin
+ * (particleSystem.h:110-112). */
+BD_API bd_status bd_get_grid(bd_handle h, int instance, uint32_t dims[3], float cell[3], float inv[3]);
+/* Poisson CDF of zeroth-order reaction rxn for one instance: P(X <= kmin+k)
+ * for k < *len (copies up to cap entries). */
+BD_API bd_status bd_get_poisson_cdf(bd_handle h, int instance, int rxn, double *cdf, size_t cap, int *kmin,
+                                    size_t *len);
+/* Diffusion coefficient of a species after the instance's scaling. */
+BD_API bd_status bd_get_species_d(bd_handle h, int instance, int species, float *D);
+/* Cell edge override before the first step (autotuner). */
+BD_API bd_status bd_set_cell_size(bd_handle h, float cell_size);
+
+/* ------------------------------------------------------------- ensemble */
+
+/* Per-instance description for a batched ensemble: every instance shares the
+ * species and reaction network of the handle but has its own box, seed,
+ * particles and parameter scaling (D x d_scale, second-order rates x
+ * k2_scale).  The reference runs one system per process; this is new. */
+typedef struct bd_instance_desc {
+  float box_lo[3], box_hi[3];
+  uint64_t seed;
+  float d_scale, k2_scale;
+  float cell_size;           /* 0 = automatic */
+  uint32_t reserved[3];
+} bd_instance_desc;
+
+/* Create an ensemble handle of n instances (species/reactions then added as
+ * for a single system). */
+BD_API bd_status bd_create_ensemble(const bd_config *cfg, const bd_instance_desc *inst,
+                                    int n_instances, bd_handle *out);
+/* Upload the particles of all instances: counts[k] particles of instance k,
+ * concatenated in instance order. */
+BD_API bd_status bd_set_ensemble_particles(bd_handle h, const float *xyz4, const int *species,
+                                           const uint64_t *counts, int n_instances);
+/* Live counts per instance (synchronises). */
+BD_API bd_status bd_get_instance_counts(bd_handle h, uint64_t *counts, int n_instances);
+/* Copy the live particles of one instance (synchronises). */
+BD_API bd_status bd_get_instance_particles(bd_handle h, int instance, float *xyz4, int *species,
+                                           size_t cap, size_t *n);
+/* Derived parameters of reaction rxn for one instance. */
+BD_API bd_status bd_get_instance_reaction_info(bd_handle h, int instance, int rxn,
+                                               bd_reaction_info *out);
+
+/* ------------------------------------------------------ rxnparam (host) */
+/* Restatements of rxnparam.h:39-42 (Andrews-Bray rate tables, rxnparam.cpp:
+ * 42-308): rate per step in length^3, binding radius, unbinding radius. */
+BD_API double bd_numrxnrate(double step, double a, double b);
+BD_API double bd_actrxnrate(double step, double a);
+BD_API double bd_bindingradius(double rate, double dt, double difc, double b, int rel);
+BD_API double bd_unbindingradius(double pgem, double dt, double difc, double a);
+/* The 4096-entry table of standard-normal quantiles used in BD_NORMALS_TABLE
+ * mode (replaces createGaussTable, stats.cpp:202-232, 277-282). */
+BD_API int bd_gauss_table(float *out, int n);
+
+BD_API const char *bd_status_string(bd_status s);
+BD_API const char *bd_version(void);
+
+#endif /* GPUSMOLDYN_H */

@@ -1,0 +1,174 @@
+"""ctypes wrapper of liboracle.so -- TEST INFRASTRUCTURE, not product.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module.  ``system_from(sys)`` reads a configured library handle's
+parameters through the public C ABI (species D, reaction table entries,
+grid, Poisson CDFs, normal table) and turns them into the oracle's inputs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+fp = C.POINTER(C.c_float)
+ip = C.POINTER(C.c_int)
+dp = C.POINTER(C.c_double)
+
+
+class or_system(C.Structure):
+    _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("inv", C.c_float * 3), ("cell", C.c_float * 3),
+                ("dims", C.c_uint32 * 3), ("key_lo", C.c_uint32), ("key_hi", C.c_uint32),
+                ("normal_mode", C.c_int), ("gauss", fp), ("S", C.c_int), ("D", fp), ("dt", C.c_float),
+                ("R", C.c_int), ("order", ip), ("react0", ip), ("react1", ip), ("prod0", ip), ("prod1", ip),
+                ("prob", fp), ("bind_radius", fp), ("off0", fp), ("off1", fp), ("cdf", dp), ("cdf_off", ip),
+                ("cdf_len", ip), ("cdf_kmin", ip), ("sorted", C.c_int), ("inst", C.c_uint32),
+                ("threads", C.c_int)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        lib = C.CDLL(path)
+        lib.or_step.restype = C.c_int
+        lib.or_step.argtypes = [C.POINTER(or_system), C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                                C.POINTER(C.c_uint32), C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint32,
+                                C.POINTER(C.c_uint32), C.c_void_p]
+        lib.or_philox.restype = None
+        lib.or_philox.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+        _lib = lib
+    return _lib
+
+
+def philox(ctr, k0, k1):
+    lib = load()
+    c = np.asarray(ctr, np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib.or_philox(c.ctypes.data, k0, k1, out.ctypes.data)
+    return out
+
+
+class OracleSystem:
+    """Oracle inputs for one instance of a library handle."""
+
+    def __init__(self, sys, instance=0, threads=0, sorted_path=None):
+        from gpusmoldyn_gb300.system import gauss_table
+
+        self.keep = []
+        d = sys.instances[instance]
+        dims, cell, inv = sys.grid(instance)
+        D = sys.species_d(instance)
+        R = sys.n_reactions
+        info = [sys.reaction_info(r, instance) for r in range(R)]
+        order = np.array([i["order"] for i in info] or [0], np.int32)
+        react0 = np.array([i["reactants"][0] for i in info] or [0], np.int32)
+        react1 = np.array([i["reactants"][1] for i in info] or [0], np.int32)
+        prod0 = np.array([i["products"][0] for i in info] or [0], np.int32)
+        prod1 = np.array([i["products"][1] for i in info] or [0], np.int32)
+        prob = np.array([i["prob"] for i in info] or [0], np.float32)
+        brad = np.array([i["bind_radius"] for i in info] or [0], np.float32)
+        off0 = np.array([i["product_offsets"][0] for i in info] or [0], np.float32)
+        off1 = np.array([i["product_offsets"][1] for i in info] or [0], np.float32)
+        cdfs, coff, clen, ckmin = [], [], [], []
+        pos = 0
+        for r in range(R):
+            if info[r]["order"] == 0:
+                cdf, kmin = sys.poisson_cdf(r, instance)
+            else:
+                cdf, kmin = np.zeros(0), 0
+            cdfs.append(cdf)
+            coff.append(pos)
+            clen.append(len(cdf))
+            ckmin.append(kmin)
+            pos += len(cdf)
+        cdf_all = np.concatenate(cdfs) if pos else np.zeros(1)
+        gauss = gauss_table()
+        arrs = dict(order=order, react0=react0, react1=react1, prod0=prod0, prod1=prod1, prob=prob,
+                    bind_radius=brad, off0=off0, off1=off1, D=D.astype(np.float32), gauss=gauss,
+                    cdf=cdf_all.astype(np.float64), cdf_off=np.array(coff or [0], np.int32),
+                    cdf_len=np.array(clen or [0], np.int32), cdf_kmin=np.array(ckmin or [0], np.int32))
+        self.arrs = arrs
+        s = or_system()
+        for a in range(3):
+            s.lo[a] = d["box_lo"][a]
+            s.hi[a] = d["box_hi"][a]
+            s.inv[a] = inv[a]
+            s.cell[a] = cell[a]
+            s.dims[a] = int(dims[a])
+        seed = int(d.get("seed", 1))
+        s.key_lo = seed & 0xFFFFFFFF
+        s.key_hi = seed >> 32
+        s.normal_mode = sys.cfg.normal_mode
+        s.S = sys.n_species
+        s.dt = sys.dt
+        s.R = R
+        for name in ("order", "react0", "react1", "prod0", "prod1", "cdf_off", "cdf_len", "cdf_kmin"):
+            setattr(s, name, arrs[name].ctypes.data_as(ip))
+        for name in ("prob", "bind_radius", "off0", "off1", "D", "gauss"):
+            setattr(s, name, arrs[name].ctypes.data_as(fp))
+        s.cdf = arrs["cdf"].ctypes.data_as(dp)
+        if sorted_path is None:
+            sorted_path = (sys.n_instances > 1 or any(i["order"] in (1, 2) for i in info)
+                           or any(i["order"] == 0 and i["nprod"] == 2 for i in info))
+        s.sorted = 1 if sorted_path else 0
+        s.inst = instance
+        s.threads = threads
+        self.s = s
+        self.n_cells = int(dims[0]) * int(dims[1]) * int(dims[2])
+        self.R = R
+
+    def step(self, t, recs, want_cells=False, want_pairs=False, cap=None, events=None):
+        """Advance records (n x 4 uint32: x, y, z bits and w) by one step."""
+        lib = load()
+        recs = np.ascontiguousarray(recs, np.uint32)
+        n = recs.shape[0]
+        cap = cap or max(4 * n + 1024, 4096)
+        out = np.zeros((cap, 4), np.uint32)
+        n_out = C.c_uint32()
+        cells = np.zeros(self.n_cells + 1, np.uint32) if want_cells else None
+        pcap = 1 << 20
+        pairs = np.zeros((pcap, 4), np.uint32) if want_pairs else None
+        n_pairs = C.c_uint32()
+        ev = events if events is not None else np.zeros(max(self.R, 1), np.uint64)
+        rc = lib.or_step(C.byref(self.s), t, recs.ctypes.data if n else None, n, out.ctypes.data, cap,
+                         C.byref(n_out), cells.ctypes.data if cells is not None else None,
+                         self.n_cells + 1, pairs.ctypes.data if pairs is not None else None, pcap,
+                         C.byref(n_pairs), ev.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"oracle step failed ({rc})")
+        res = dict(recs=out[:n_out.value].copy(), events=ev)
+        if want_cells:
+            res["cells"] = cells
+        if want_pairs:
+            res["pairs"] = pairs[:n_pairs.value].copy()
+        return res
+
+
+def records(pos, species, inst=0):
+    """Pack (n,3) float32 positions and species into oracle records."""
+    pos = np.asarray(pos, np.float32)
+    n = pos.shape[0]
+    r = np.zeros((n, 4), np.uint32)
+    r[:, :3] = pos[:, :3].view(np.uint32)
+    r[:, 3] = (np.uint32(inst) << np.uint32(16)) | np.asarray(species, np.uint32)
+    return r
+
+
+def slots_to_records(xyz, w):
+    r = np.zeros((xyz.shape[0], 4), np.uint32)
+    r[:, :3] = np.ascontiguousarray(xyz, np.float32).view(np.uint32)
+    r[:, 3] = w
+    dead = w == 0xFFFFFFFF
+    r[dead, :3] = 0
+    return r
+
+
+def default_threads():
+    return int(os.environ.get("ORACLE_THREADS", "0"))
