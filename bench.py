@@ -1,0 +1,433 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 Brownian-dynamics step, one JSON line on stdout.
+
+Metric: particle-steps/s (live particles advanced per second, summed over
+steps), the reference's benchmark quantity (particles.cpp:213-226 times
+update() over N particles and I iterations).
+
+Headline workload ("c3"): the plain 16M-particle, 8-species network in a
+200 um reflecting cube with 12 reactions (dt 1 ms), seeded synthetic
+positions.  The state (16M x 16 B = 256 MB) is larger than the 129 MB L2,
+so no flush is needed between timed steps.  `value` is timed on the device
+with CUDA events on the library's own stream over exactly --steps graph
+launches after --warmup untimed ones; `e2e` runs the same workload through
+the public C ABI with host buffers (upload, one step + a live-count readback
+per step, download); `batched` times the 256-instance ensemble (c4) as one
+pipeline per step and the same instances stepped one by one as plain systems.
+
+--impl reference times the CPU restatement of the reference's step (the
+reference has no CPU step of its own and its CUDA 2.x code does not build
+with CUDA 13) on the host cores, on a bounded sample of the same workload.
+
+Multi-GPU (--gpus N under torchrun): instances are independent, so each
+rank advances its own replica of the workload on its own GPU; the ranks only
+meet at the barriers around the timed region (no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s plain vs batched ensemble on 1 GB300 at <1% rate/MSD error; p99"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="c3", choices=["c3", "c2"])
+    p.add_argument("--n", type=int, default=0, help="override the particle count (debug)")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--profile-only", action="store_true", help="build + a few steps (for ncu)")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------- distribution
+class Dist:
+    def __init__(self, want):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+# ---------------------------------------------------------------- roofline
+def measured_peak():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def algorithmic_bytes(kernel, n_in, n_out, n_cells):
+    """Bytes a kernel must move at minimum (16-byte records, 4-byte cell words)."""
+    table = {
+        "k_count": 16 * n_in + 4 * n_cells,                 # read records, write histogram
+        "k_scan_tiles": 4 * n_cells,
+        "k_scan_down": 8 * n_cells,                          # read counts, write starts
+        "k_scatter": 16 * n_in + 16 * n_out + 8 * n_cells,   # read + write records, starts + counts
+        "k_pairs": 32 * n_out + 4 * n_cells,                 # read + write records, starts
+        "k_diffuse": 32 * n_in,
+    }
+    return table.get(kernel)
+
+
+# -------------------------------------------------------------- workloads
+def build_workload(name, n_override=0, normals="boxmuller", device=0, host_only=False):
+    from gpusmoldyn_gb300 import configs
+
+    dev = -1 if host_only else device
+    if name == "c3":
+        n = n_override or 16_000_000
+        side = 200.0 * (n / 16_000_000) ** (1 / 3)
+        return configs.build_c3(n=n, side=side, normals=normals, device=dev), f"c3: {n} particles, 8 species, " \
+            f"12 reactions, {side:.1f} um reflecting cube, dt 1 ms"
+    n = n_override or 1_000_000
+    side = 60.0 * (n / 1_000_000) ** (1 / 3)
+    return configs.build_c2(n_a=n // 2, n_b=n - n // 2, side=side, normals=normals, device=dev), \
+        f"c2: {n} particles, A+B<->C, {side:.1f} um cube, dt 0.5 ms"
+
+
+def network_and_particles(name, n_override, device):
+    """A finalized handle without particles, and the initial state as host arrays."""
+    from gpusmoldyn_gb300 import configs
+
+    if name == "c3":
+        n = n_override or 16_000_000
+        side = 200.0 * (n / 16_000_000) ** (1 / 3)
+        s = configs.c3_system(n=n, side=side, device=device)
+        pos, sp = configs.c3_particles(n, side)
+    else:
+        n = n_override or 1_000_000
+        side = 60.0 * (n / 1_000_000) ** (1 / 3)
+        s = configs.c2_system(side=side, device=device)
+        pos, sp = configs.c2_particles(n // 2, n - n // 2, side)
+    return s, pos, sp
+
+
+def c3_sample_system(n, host_only=True, seed=3):
+    """The c3 network at the c3 density in a smaller cube."""
+    from gpusmoldyn_gb300 import configs
+
+    side = (n / 2.0) ** (1 / 3)
+    return configs.build_c3(n=n, side=side, seed=seed, device=-1 if host_only else 0), side
+
+
+def cpu_oracle_rate(n, steps, threads, budget_s=None):
+    """Particle-steps/s of the CPU restatement on a c3-network sample."""
+    import numpy as np
+
+    from oracle import py as orc
+
+    s, side = c3_sample_system(n)
+    o = orc.OracleSystem(s, threads=threads)
+    from gpusmoldyn_gb300 import configs
+
+    g = configs.rng(3)
+    pos = configs.uniform_positions(g, n, (0, 0, 0), (side, side, side))
+    sp = (np.arange(n) % 8).astype(np.int32)
+    recs = orc.records(pos, sp)
+    recs = o.step(0, recs)["recs"]  # warm-up
+    done = 0
+    psteps = 0
+    t0 = time.perf_counter()
+    for t in range(1, steps + 1):
+        live = int(np.sum(recs[:, 3] != 0xFFFFFFFF))
+        recs = o.step(t, recs)["recs"]
+        psteps += live
+        done += 1
+        if budget_s and time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    s.close()
+    return psteps / el, done, el, side
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    n = 262144 if args.steps <= 200 else 65536
+    for _ in range(max(args.warmup, 0)):
+        pass
+    rate, done, el, side = cpu_oracle_rate(n, args.steps, threads)
+    sample = (f"c3 network at the c3 density: {n} particles in a {side:.1f} um cube, {done} steps "
+              f"({el:.1f} s), OpenMP {threads} threads")
+    return {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": done, "warmup": 1, "ms_per_step": el / max(done, 1) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c3 (sampled, see cpu_baseline.sample)", "seq_len": None, "global_batch": None,
+                   "parallelism": "cpu"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_gb300(args, dist):
+    import numpy as np
+
+    import gpusmoldyn_gb300
+    from gpusmoldyn_gb300 import build as libbuild
+    from gpusmoldyn_gb300 import configs
+
+    libbuild.build()
+    gpusmoldyn_gb300.load()
+    device = dist.local
+    # ---------------- headline: device-timed plain step
+    s, desc = build_workload(args.workload, args.n, device=device)
+    s.step(args.warmup)
+    s.synchronize()
+    n0 = s.count()
+    dims, cell, inv = s.grid()
+    n_cells = int(np.prod(dims.astype(np.int64)))
+    if args.profile_only:
+        s.step(3)
+        s.synchronize()
+        print(json.dumps({"profile_only": True, "n": n0}))
+        return None
+    clocks = ClockSampler(device)
+    dist.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    ms = s.time_steps(args.steps)
+    clk = clocks.stop()
+    dist.barrier()
+    n1 = s.count()
+    ms_max = dist.max(ms)
+    local_ps = args.steps * 0.5 * (n0 + n1)
+    total_ps = dist.sum(local_ps)
+    value = total_ps / (ms_max / 1e3)
+    kps = s.kernels_per_step()
+    # per-kernel device times (events between kernels, outside the timed region)
+    prof_steps = 20
+    prof = s.profile_steps(prof_steps)
+    dom = max(prof, key=prof.get)
+    n_now = s.count()
+    alg = algorithmic_bytes(dom, n_now, n_now, n_cells)
+    peak, peak_kind = measured_peak()
+    roof = None
+    if alg:
+        achieved = alg / (prof[dom] / prof_steps / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": alg,
+                "traffic": traffic_from_profiles(dom, args.workload)}
+    step_alg = sum(v for v in (algorithmic_bytes(k, n_now, n_now, n_cells) for k in prof) if v)
+    step_roof = {"bytes_per_step": step_alg, "achieved_gbs": step_alg / (ms / args.steps / 1e3) / 1e9,
+                 "frac": step_alg / (ms / args.steps / 1e3) / 1e9 / peak}
+    s.close()
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox uniform positions)",
+        "config": {"workload": desc, "global_batch": int(n0) * dist.world, "seq_len": None,
+                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
+                   "normals": "box-muller (Philox)", "cells": n_cells, "l2": "state 256 MB > 129 MB L2, no flush"},
+        "clocks": clk, "gpu_launches": kps * args.steps,
+        "kernel_ms_per_step": {k: v / prof_steps for k, v in prof.items()},
+        "roofline": roof, "step_roofline": step_roof,
+    }
+
+    # ---------------- end to end through the C ABI with host buffers
+    if not args.no_e2e:
+        s3, pos, sp = network_and_particles(args.workload, args.n, device)
+        dist.barrier()
+        t0 = time.perf_counter()
+        s3.set_particles(pos, sp)
+        psteps = 0
+        live = len(sp)
+        for _ in range(args.steps):
+            s3.step(1)
+            live = s3.count()
+            psteps += live
+        pos_out, sp_out = s3.particles()
+        t1 = time.perf_counter()
+        dist.barrier()
+        e2e_s = dist.max(t1 - t0)
+        out["e2e"] = {"value": dist.sum(psteps) / e2e_s, "unit": UNIT,
+                      "h2d_bytes_per_step": 20 * len(sp) / args.steps,
+                      "d2h_bytes_per_step": 8 + 20 * len(sp_out) / args.steps,
+                      "path": "bd_set_particles + steps x (bd_step(1) + bd_get_count) + bd_get_particles"}
+        s3.close()
+
+    # ---------------- batched ensemble vs the plain per-instance loop
+    if not args.no_batched:
+        out["batched"] = run_batched(args, dist, device)
+
+    # ---------------- CPU baseline (rank 0, N = 1 only)
+    if not args.no_cpu and dist.rank == 0 and dist.world == 1:
+        threads = os.cpu_count() or 1
+        rate, done, el, side = cpu_oracle_rate(262144, 200, threads, budget_s=20.0)
+        out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"c3 network at the c3 density: 262144 particles in a {side:.1f} um cube,"
+                                         f" {done} steps ({el:.1f} s), OpenMP {threads} threads"}
+    return out
+
+
+def run_batched(args, dist, device):
+    import numpy as np
+
+    from gpusmoldyn_gb300 import configs
+
+    steps = max(args.steps // 4, 20)
+    s, inst, counts = configs.build_c4(device=device)
+    s.step(args.warmup)
+    s.synchronize()
+    n0 = int(np.sum(s.instance_counts()))
+    ms = s.time_steps(steps)
+    n1 = int(np.sum(s.instance_counts()))
+    batched = steps * 0.5 * (n0 + n1) / (ms / 1e3)
+    s.close()
+    # the same instances advanced one after another as plain systems
+    loop_steps = 10
+    total_ms = 0.0
+    total_ps = 0.0
+    pos, sp = configs.c4_positions(inst, counts)
+    off = 0
+    for d, n in zip(inst, counts):
+        p = configs.build_c2_instance(d, n, device=device)
+        p.set_particles(pos[off:off + n], sp[off:off + n])
+        off += n
+        p.step(3)
+        p.synchronize()
+        total_ms += p.time_steps(loop_steps)
+        total_ps += loop_steps * int(n)
+        p.close()
+    loop = total_ps / (total_ms / 1e3)
+    return {"workload": f"c4: {len(inst)} instances of the c2 network, {int(np.sum(counts))} particles",
+            "value": batched, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
+            "plain_loop_value": loop, "speedup_vs_plain_loop": batched / loop}
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    try:
+        if args.impl == "reference":
+            out = run_reference(args, dist)
+        else:
+            out = run_gb300(args, dist)
+        if out is not None and dist.rank == 0:
+            print(json.dumps(out))
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

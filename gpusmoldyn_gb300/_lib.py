@@ -82,12 +82,17 @@ _SIGS = {
     "bd_get_particles": (C.c_int, [H, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_get_instance_particles": (C.c_int, [H, C.c_int, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_get_instance_counts": (C.c_int, [H, P, C.c_int]),
+    "bd_get_species_counts": (C.c_int, [H, C.c_int, P, C.c_int]),
     "bd_get_state_pointer": (C.c_int, [H, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)]),
     "bd_step": (C.c_int, [H, C.c_int]),
     "bd_synchronize": (C.c_int, [H]),
     "bd_get_step": (C.c_int, [H, C.POINTER(C.c_uint64)]),
     "bd_get_event_counts": (C.c_int, [H, P, C.c_int]),
     "bd_get_stage_times": (C.c_int, [H, P, C.c_int]),
+    "bd_time_steps": (C.c_int, [H, C.c_int, C.POINTER(C.c_float)]),
+    "bd_profile_steps": (C.c_int, [H, C.c_int, P, C.c_int, C.POINTER(C.c_int)]),
+    "bd_stage_name": (C.c_char_p, [H, C.c_int]),
+    "bd_get_kernels_per_step": (C.c_int, [H, C.POINTER(C.c_int)]),
     "bd_debug_get_slots": (C.c_int, [H, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_debug_get_cells": (C.c_int, [H, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_debug_get_pairs": (C.c_int, [H, P, C.c_size_t, C.POINTER(C.c_size_t)]),

@@ -57,14 +57,23 @@ def c2_network(s, kon=0.05, koff=10.0):
     return A, B, Cc, fwd, back
 
 
-def build_c2(n_a=500000, n_b=500000, side=60.0, seed=2, normals="boxmuller", **kw):
+def c2_system(side=60.0, seed=2, normals="boxmuller", **kw):
     s = System((0, 0, 0), (side, side, side), dt=5e-4, seed=seed, normals=normals, **kw)
-    A, B, Cc, _, _ = c2_network(s)
+    c2_network(s)
     s.finalize()
+    return s
+
+
+def c2_particles(n_a=500000, n_b=500000, side=60.0, seed=2):
     g = rng(seed)
     pos = uniform_positions(g, n_a + n_b, (0, 0, 0), (side, side, side))
-    sp = np.concatenate([np.full(n_a, A), np.full(n_b, B)]).astype(np.int32)
-    s.set_particles(pos, sp)
+    sp = np.concatenate([np.zeros(n_a), np.ones(n_b)]).astype(np.int32)
+    return pos, sp
+
+
+def build_c2(n_a=500000, n_b=500000, side=60.0, seed=2, normals="boxmuller", **kw):
+    s = c2_system(side, seed, normals, **kw)
+    s.set_particles(*c2_particles(n_a, n_b, side, seed))
     return s
 
 
@@ -105,7 +114,8 @@ def c3_zeroth_rate(D, rx, density):
     return loss / 2.0
 
 
-def build_c3(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
+def c3_system(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
+    """The c3 network in a `side` cube, finalized, without particles."""
     s = System((0, 0, 0), (side, side, side), dt=1e-3, seed=seed, normals=normals, **kw)
     D, rx = c3_network(network_seed)
     for d in D:
@@ -116,10 +126,19 @@ def build_c3(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed
     for order, rc, pr, k in rx:
         s.add_reaction(order, rc, pr, float(k))
     s.finalize()
+    return s
+
+
+def c3_particles(n=16_000_000, side=200.0, seed=3):
     g = rng(seed)
     pos = uniform_positions(g, n, (0, 0, 0), (side, side, side))
     sp = (np.arange(n) % 8).astype(np.int32)
-    s.set_particles(pos, sp)
+    return pos, sp
+
+
+def build_c3(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
+    s = c3_system(n, side, seed, normals, network_seed, **kw)
+    s.set_particles(*c3_particles(n, side, seed))
     return s
 
 

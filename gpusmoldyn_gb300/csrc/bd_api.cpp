@@ -108,6 +108,7 @@ struct bd_system {
   LaunchShape shape{};
 
   bool host_only = false;  // BD_DEVICE_NONE: parameters and grid only
+  std::vector<std::string> stage_names;  // kernels of one step (bd_profile_steps)
 
   bool diffuse_only() const { return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products; }
   int n_inst() const { return (int)idesc.size(); }
@@ -886,6 +887,29 @@ BD_API bd_status bd_get_instance_counts(bd_handle h, uint64_t* counts, int n_ins
   return BD_OK;
 }
 
+BD_API bd_status bd_get_species_counts(bd_handle h, int inst, uint64_t* counts, int n) {
+  if (!h || !counts || n < 0 || inst < -1 || inst >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  for (int s = 0; s < n; s++) counts[s] = 0;
+  if (!h->have_particles) return BD_OK;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const size_t m = (size_t)h->n_inst() * h->S;
+  DevBuf<unsigned long long> d;
+  BD_CUDA(d.alloc(m));
+  BD_CUDA(cudaMemsetAsync(d.p, 0, m * sizeof(unsigned long long), h->stream));
+  enqueue_species_counts(make_params(h), d.p, h->stream);
+  BD_CUDA(cudaGetLastError());
+  std::vector<unsigned long long> hv(m);
+  BD_CUDA(cudaMemcpyAsync(hv.data(), d.p, m * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  d.free();
+  for (int k = 0; k < h->n_inst(); k++) {
+    if (inst >= 0 && k != inst) continue;
+    for (int s = 0; s < std::min(n, h->S); s++) counts[s] += hv[(size_t)k * h->S + s];
+  }
+  return BD_OK;
+}
+
 BD_API bd_status bd_get_event_counts(bd_handle h, uint64_t* counts, int n) {
   if (!h || !counts || n < 0) return BD_ERR_INVALID_ARGUMENT;
   for (int r = 0; r < n; r++) counts[r] = 0;
@@ -897,6 +921,94 @@ BD_API bd_status bd_get_event_counts(bd_handle h, uint64_t* counts, int n) {
   BD_CUDA(cudaMemcpy(ev.data(), h->events.p, ev.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   for (int k = 0; k < I; k++)
     for (int r = 0; r < std::min(n, h->R); r++) counts[r] += ev[(size_t)k * R + r];
+  return BD_OK;
+}
+
+BD_API bd_status bd_time_steps(bd_handle h, int nsteps, float* ms) {
+  if (!h || !ms || nsteps < 0) return BD_ERR_INVALID_ARGUMENT;
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  BD_CUDA(cudaSetDevice(h->device));
+  cudaEvent_t e0, e1;
+  BD_CUDA(cudaEventCreate(&e0));
+  BD_CUDA(cudaEventCreate(&e1));
+  BD_CUDA(cudaEventRecord(e0, h->stream));
+  bd_status st = bd_step(h, nsteps);
+  if (!st) {
+    BD_CUDA(cudaEventRecord(e1, h->stream));
+    BD_CUDA(cudaEventSynchronize(e1));
+    BD_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  return bd_synchronize(h);
+}
+
+namespace {
+struct ProfileCtx {
+  cudaStream_t stream;
+  std::vector<cudaEvent_t>* events;
+  std::vector<std::string>* names;
+  bool record_names;
+};
+void profile_hook(void* c, const char* name) {
+  ProfileCtx* p = (ProfileCtx*)c;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, p->stream);
+  p->events->push_back(e);
+  if (p->record_names) p->names->push_back(name);
+}
+}  // namespace
+
+BD_API bd_status bd_profile_steps(bd_handle h, int nsteps, float* stage_ms, int cap, int* n_stages) {
+  if (!h || nsteps < 1 || !n_stages) return BD_ERR_INVALID_ARGUMENT;
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  if (!h->finalized || !h->have_particles) return BD_ERR_NOT_FINALIZED;
+  BD_CUDA(cudaSetDevice(h->device));
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const KParams p = make_params(h);
+  const bool table = h->cfg.normal_mode == BD_NORMALS_TABLE;
+  const Path path = h->diffuse_only() ? Path::kDiffuseOnly : Path::kSorted;
+  std::vector<float> acc;
+  h->stage_names.clear();
+  for (int k = 0; k < nsteps; k++) {
+    std::vector<cudaEvent_t> ev;
+    cudaEvent_t e0;
+    BD_CUDA(cudaEventCreate(&e0));
+    BD_CUDA(cudaEventRecord(e0, h->stream));
+    ev.push_back(e0);
+    ProfileCtx ctx{h->stream, &ev, &h->stage_names, k == 0};
+    const int nk = enqueue_step(p, path, table, h->Z > 0, h->U > 0, h->B > 0, h->shape, h->stream, profile_hook,
+                                &ctx);
+    BD_CUDA(cudaGetLastError());
+    BD_CUDA(cudaEventSynchronize(ev.back()));
+    if (acc.empty()) acc.assign(nk, 0.0f);
+    for (int s = 0; s < nk && s + 1 < (int)ev.size(); s++) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[s], ev[s + 1]);
+      acc[s] += ms;
+    }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    h->target_step += 1;
+  }
+  *n_stages = (int)acc.size();
+  if (stage_ms)
+    for (int s = 0; s < (int)acc.size() && s < cap; s++) stage_ms[s] = acc[s];
+  st = bd_synchronize(h);
+  return st == BD_ERR_EMPTY ? BD_OK : st;
+}
+
+BD_API const char* bd_stage_name(bd_handle h, int k) {
+  if (!h || k < 0 || k >= (int)h->stage_names.size()) return "";
+  return h->stage_names[k].c_str();
+}
+
+BD_API bd_status bd_get_kernels_per_step(bd_handle h, int* n) {
+  if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
+  if (h->diffuse_only()) *n = (h->Z > 0 ? 2 : 0) + 2;
+  else *n = (h->Z > 0 ? 1 : 0) + 7;
   return BD_OK;
 }
 

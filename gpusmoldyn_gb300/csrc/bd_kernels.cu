@@ -668,34 +668,78 @@ __global__ void __launch_bounds__(256) k_instance_counts(KParams p, unsigned lon
   }
 }
 
+__global__ void __launch_bounds__(256) k_species_counts(KParams p, unsigned long long* counts) {
+  const DevCtrl* c = p.ctrl;
+  const uint32_t cur = ld_u32(&c->cur);
+  const float4* st = cur_state(p, cur);
+  const uint32_t n = ld_u32(&c->n_slots);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t key = kNoKey;
+    if (i < n) {
+      const uint32_t w = rec_w(st[i]);
+      if (w != kDead) key = (w >> 16) * p.S + (w & 0xFFFFu);
+    }
+    const uint32_t peers = __match_any_sync(kFull, key);
+    if (key != kNoKey && lane_id() == (uint32_t)(__ffs(peers) - 1))
+      atomicAdd(&counts[key], (unsigned long long)__popc(peers));
+  }
+}
+
 }  // namespace
 
-void enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
-                  const LaunchShape& shape, cudaStream_t s) {
+int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
+                 const LaunchShape& shape, cudaStream_t s, StageHook hook, void* ctx) {
   (void)has_uni;
   const int gs = shape.grid_stream, bs = shape.block_stream;
-  if (has_zero) k_zeroth<<<1, 1024, 0, s>>>(p, path == Path::kDiffuseOnly ? 1 : 0);
+  int n = 0;
+  auto done = [&](const char* name) {
+    ++n;
+    if (hook) hook(ctx, name);
+  };
+  if (has_zero) {
+    k_zeroth<<<1, 1024, 0, s>>>(p, path == Path::kDiffuseOnly ? 1 : 0);
+    done("k_zeroth");
+  }
   if (path == Path::kDiffuseOnly) {
     if (table) k_diffuse<true><<<gs, bs, 0, s>>>(p);
     else k_diffuse<false><<<gs, bs, 0, s>>>(p);
-    if (has_zero) k_append<<<gs, bs, 0, s>>>(p);
+    done("k_diffuse");
+    if (has_zero) {
+      k_append<<<gs, bs, 0, s>>>(p);
+      done("k_append");
+    }
     k_finalize_inplace<<<1, 256, 0, s>>>(p);
-    return;
+    done("k_finalize_inplace");
+    return n;
   }
   if (table) k_count<true><<<gs, bs, 0, s>>>(p);
   else k_count<false><<<gs, bs, 0, s>>>(p);
+  done("k_count");
   k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
+  done("k_scan_tiles");
   k_scan_top<<<1, 1024, 0, s>>>(p);
+  done("k_scan_top");
   k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
+  done("k_scan_down");
   if (table) k_scatter<true><<<gs, bs, 0, s>>>(p);
   else k_scatter<false><<<gs, bs, 0, s>>>(p);
+  done("k_scatter");
   if (has_bim) k_pairs<true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
   else k_pairs<false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+  done("k_pairs");
   k_match<<<1, 1024, 0, s>>>(p);
+  done("k_match");
+  return n;
 }
 
 void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaStream_t s) {
   k_instance_counts<<<152 * 4, 256, 0, s>>>(p, counts);
+}
+
+void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaStream_t s) {
+  k_species_counts<<<152 * 4, 256, 0, s>>>(p, counts);
 }
 
 }  // namespace bd

@@ -44,12 +44,19 @@ struct LaunchShape {
   int grid_pairs, block_pairs;
 };
 
+// Called after each kernel of a step is enqueued (stage name); lets the
+// profiler record an event between kernels.  nullptr = no callback.
+typedef void (*StageHook)(void* ctx, const char* stage);
+
 // Enqueue one full step on `stream`.  table selects the normal generator.
-void enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
-                  const LaunchShape& shape, cudaStream_t stream);
+// Returns the number of kernels enqueued.
+int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
+                 const LaunchShape& shape, cudaStream_t stream, StageHook hook = nullptr, void* ctx = nullptr);
 
 // Count live records per instance (counts[I] must be zeroed).
 void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaStream_t stream);
+// Count live records per (instance, species): counts[I * S] must be zeroed.
+void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaStream_t stream);
 
 // Tile size of the cell scan.
 constexpr uint32_t kScanTile = 4096;

@@ -158,6 +158,11 @@ class System:
         m = min(got.value, n)
         return pos[:m, :3].copy(), sp[:m].copy()
 
+    def species_counts(self, instance=-1) -> np.ndarray:
+        out = np.zeros(max(self.n_species, 1), np.uint64)
+        L.check(self.lib.bd_get_species_counts(self.h, instance, _ptr(out), self.n_species), "species_counts")
+        return out[:self.n_species]
+
     def instance_counts(self) -> np.ndarray:
         out = np.zeros(self.n_instances, np.uint64)
         L.check(self.lib.bd_get_instance_counts(self.h, _ptr(out), self.n_instances), "instance_counts")
@@ -196,6 +201,24 @@ class System:
         out = np.zeros(max(self.n_reactions, 1), np.uint64)
         L.check(self.lib.bd_get_event_counts(self.h, _ptr(out), self.n_reactions), "event_counts")
         return out[:self.n_reactions]
+
+    def time_steps(self, n) -> float:
+        """Device time in ms of n steps (CUDA events on the handle's stream)."""
+        ms = C.c_float()
+        L.check(self.lib.bd_time_steps(self.h, int(n), C.byref(ms)), "bd_time_steps", ok=(L.BD_OK, L.BD_ERR_EMPTY))
+        return ms.value
+
+    def profile_steps(self, n):
+        """Summed device time per kernel over n steps: {kernel name: ms}."""
+        buf = np.zeros(32, np.float32)
+        k = C.c_int()
+        L.check(self.lib.bd_profile_steps(self.h, int(n), _ptr(buf), 32, C.byref(k)), "bd_profile_steps")
+        return {self.lib.bd_stage_name(self.h, i).decode(): float(buf[i]) for i in range(k.value)}
+
+    def kernels_per_step(self) -> int:
+        k = C.c_int()
+        L.check(self.lib.bd_get_kernels_per_step(self.h, C.byref(k)), "kernels_per_step")
+        return k.value
 
     def state_pointer(self):
         p = C.c_void_p()

@@ -196,8 +196,24 @@ BD_API bd_status bd_get_step(bd_handle h, uint64_t *step);
 /* Cumulative event count per reaction (n entries). */
 BD_API bd_status bd_get_event_counts(bd_handle h, uint64_t *counts, int n);
 
-/* Per-step kernel time breakdown of the last bd_step batch, in ms
- * (diagnostics; zeros unless BD_TIMING=1 in the environment). */
+/* Run nsteps timesteps (as bd_step) bracketed by CUDA events recorded on the
+ * handle's stream; *ms receives the device time between them.  Synchronises.
+ * The reference times update() with a host timer around
+ * cudaThreadSynchronize (particles.cpp:213-226). */
+BD_API bd_status bd_time_steps(bd_handle h, int nsteps, float *ms);
+
+/* Run nsteps timesteps launching the kernels one by one with a CUDA event
+ * between consecutive kernels; stage_ms[k] receives the summed device time
+ * of kernel k of the step (n_stages of them, at most cap).  Diagnostics for
+ * the per-kernel roofline; the production path launches graphs. */
+BD_API bd_status bd_profile_steps(bd_handle h, int nsteps, float *stage_ms, int cap, int *n_stages);
+/* Name of kernel k of the step, as profiled by bd_profile_steps. */
+BD_API const char *bd_stage_name(bd_handle h, int k);
+
+/* Kernel launches in one timestep of the current configuration. */
+BD_API bd_status bd_get_kernels_per_step(bd_handle h, int *n);
+
+/* Unused; kept for layout stability of older callers.  Zero-fills ms. */
 BD_API bd_status bd_get_stage_times(bd_handle h, float *ms, int n);
 
 /* --------------------------------------------------- parity / inspection */
@@ -244,6 +260,11 @@ BD_API bd_status bd_create_ensemble(const bd_config *cfg, const bd_instance_desc
  * concatenated in instance order. */
 BD_API bd_status bd_set_ensemble_particles(bd_handle h, const float *xyz4, const int *species,
                                            const uint64_t *counts, int n_instances);
+/* Live particles per species (synchronises): counts[s] for s < n, summed
+ * over instances (instance = -1) or for one instance.  Replaces reading
+ * the whole type array back (particles.cpp:509-552 debug dumps). */
+BD_API bd_status bd_get_species_counts(bd_handle h, int instance, uint64_t *counts, int n);
+
 /* Live counts per instance (synchronises). */
 BD_API bd_status bd_get_instance_counts(bd_handle h, uint64_t *counts, int n_instances);
 /* Copy the live particles of one instance (synchronises). */
