@@ -227,7 +227,7 @@ def c3_sample_system(n, host_only=True, seed=3):
     return configs.build_c3(n=n, side=side, seed=seed, device=-1 if host_only else 0), side
 
 
-def cpu_oracle_rate(n, steps, threads, budget_s=None):
+def cpu_oracle_rate(n, steps, threads, budget_s=None, warmup=1):
     """Particle-steps/s of the CPU restatement on a c3-network sample."""
     import numpy as np
 
@@ -241,11 +241,12 @@ def cpu_oracle_rate(n, steps, threads, budget_s=None):
     pos = configs.uniform_positions(g, n, (0, 0, 0), (side, side, side))
     sp = (np.arange(n) % 8).astype(np.int32)
     recs = orc.records(pos, sp)
-    recs = o.step(0, recs)["recs"]  # warm-up
+    for t in range(max(warmup, 1)):
+        recs = o.step(t, recs)["recs"]
     done = 0
     psteps = 0
     t0 = time.perf_counter()
-    for t in range(1, steps + 1):
+    for t in range(max(warmup, 1), max(warmup, 1) + steps):
         live = int(np.sum(recs[:, 3] != 0xFFFFFFFF))
         recs = o.step(t, recs)["recs"]
         psteps += live
@@ -262,17 +263,15 @@ def run_reference(args, dist):
         return None
     threads = os.cpu_count() or 1
     n = 262144 if args.steps <= 200 else 65536
-    for _ in range(max(args.warmup, 0)):
-        pass
-    rate, done, el, side = cpu_oracle_rate(n, args.steps, threads)
+    rate, done, el, side = cpu_oracle_rate(n, args.steps, threads, warmup=args.warmup)
     sample = (f"c3 network at the c3 density: {n} particles in a {side:.1f} um cube, {done} steps "
-              f"({el:.1f} s), OpenMP {threads} threads")
+              f"({el:.1f} s) after {max(args.warmup, 1)} warm-up, OpenMP {threads} threads")
     return {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": done, "warmup": 1, "ms_per_step": el / max(done, 1) * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c3 (sampled, see cpu_baseline.sample)", "seq_len": None, "global_batch": None,
-                   "parallelism": "cpu"},
+        "steps": done, "warmup": max(args.warmup, 1), "ms_per_step": el / max(done, 1) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Philox uniform positions)",
+        "config": {"workload": "c3 network, sampled (see cpu_baseline.sample)", "parallelism": "cpu"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -336,7 +335,7 @@ def run_gb300(args, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox uniform positions)",
-        "config": {"workload": desc, "global_batch": int(n0) * dist.world, "seq_len": None,
+        "config": {"workload": desc, "particles": int(n0) * dist.world,
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
                    "normals": "box-muller (Philox)", "cells": n_cells, "l2": "state 256 MB > 129 MB L2, no flush"},
         "clocks": clk, "gpu_launches": kps * args.steps,

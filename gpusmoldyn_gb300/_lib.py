@@ -101,6 +101,12 @@ _SIGS = {
                                      C.POINTER(C.c_size_t)]),
     "bd_get_species_d": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "bd_set_cell_size": (C.c_int, [H, C.c_float]),
+    "bd_create_server": (C.c_int, [C.POINTER(bd_config), C.c_int, C.POINTER(H)]),
+    "bd_instance_admit": (C.c_int, [H, C.POINTER(bd_instance_desc), P, P, C.c_size_t, C.c_uint32,
+                                    C.POINTER(C.c_int)]),
+    "bd_instance_poll": (C.c_int, [H, P, C.c_int, C.POINTER(C.c_int)]),
+    "bd_instance_harvest": (C.c_int, [H, C.c_int, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "bd_instance_state": (C.c_int, [H, C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "bd_numrxnrate": (C.c_double, [C.c_double, C.c_double, C.c_double]),
     "bd_actrxnrate": (C.c_double, [C.c_double, C.c_double]),
     "bd_bindingradius": (C.c_double, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),

@@ -110,7 +110,16 @@ struct bd_system {
   bool host_only = false;  // BD_DEVICE_NONE: parameters and grid only
   std::vector<std::string> stage_names;  // kernels of one step (bd_profile_steps)
 
-  bool diffuse_only() const { return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products; }
+  // serving: instance slots filled and emptied while the handle runs
+  bool server = false;
+  std::vector<uint8_t> slot_used;        // admitted, not yet harvested
+  std::vector<uint64_t> slot_free_after; // removed: free once ctrl.step exceeds this
+  std::vector<uint32_t> h_flags, h_target;
+  DevBuf<uint32_t> inst_flags, inst_target;
+
+  bool diffuse_only() const {
+    return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products && !server;
+  }
   int n_inst() const { return (int)idesc.size(); }
 };
 
@@ -137,6 +146,8 @@ KParams make_params(bd_system* h) {
   p.bim_table = h->dtable.p;
   p.gauss = h->dgauss.p;
   p.inst_step = h->inst_step.p;
+  p.inst_flags = h->inst_flags.p;
+  p.inst_target = h->inst_target.p;
   p.inst_slot_base = h->inst_slot_base.p;
   p.zero_off = h->zero_off.p;
   p.cell_count = h->cell_count.p;
@@ -345,20 +356,36 @@ bd_status grow_pairs(bd_system* h, uint32_t cap) {
   return BD_OK;
 }
 
-// Grid, cell arrays and instance table for the current particle counts.
-bd_status setup_grid(bd_system* h, const std::vector<uint64_t>& counts) {
+// Grid and Philox key of instance k, planned from its particle count.  An
+// instance keeps its grid for life: the cell grid decides the canonical
+// order, so it must not depend on the other instances.
+void plan_instance(bd_system* h, int k, uint64_t n) {
+  DevInstance& D = h->hinst[k];
+  choose_grid(h, k, n, &D);
+  D.key_lo = (uint32_t)(h->idesc[k].seed & 0xFFFFFFFFu);
+  D.key_hi = (uint32_t)(h->idesc[k].seed >> 32);
+  D.block = (uint32_t)k;
+  D.flags = kInstActive;
+}
+
+// Consecutive cell ranges for the instances in instance order (unused
+// server slots get a single cell), the cell arrays and the instance table.
+bd_status layout_cells(bd_system* h) {
   const int I = h->n_inst();
-  h->hinst.assign(I, DevInstance{});
   uint64_t base = 0;
   for (int k = 0; k < I; k++) {
     DevInstance& D = h->hinst[k];
-    choose_grid(h, k, counts[k], &D);
+    if (h->server && !h->slot_used[k]) {
+      for (int a = 0; a < 3; a++) {
+        D.dims[a] = 1;
+        D.lo[a] = 0.0f;
+        D.hi[a] = 1.0f;
+        D.cell[a] = 1.0f;
+        D.inv[a] = 1.0f;
+      }
+    }
     D.cell_base = (uint32_t)base;
     base += (uint64_t)D.dims[0] * D.dims[1] * D.dims[2];
-    D.key_lo = (uint32_t)(h->idesc[k].seed & 0xFFFFFFFFu);
-    D.key_hi = (uint32_t)(h->idesc[k].seed >> 32);
-    D.block = (uint32_t)k;
-    D.flags = kInstActive;
   }
   if (base > 0xFFFFFFF0ull) return BD_ERR_CAPACITY;
   h->n_cells = (uint32_t)base;
@@ -400,8 +427,9 @@ bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, 
       recs[i] = make_float4(x, y, z, wf);
     }
   }
-  std::vector<uint64_t> cvec(counts, counts + I);
-  bd_status st = setup_grid(h, cvec);
+  h->hinst.assign(I, DevInstance{});
+  for (int k = 0; k < I; k++) plan_instance(h, k, counts[k]);
+  bd_status st = layout_cells(h);
   if (st) return st;
   if (h->host_only) return BD_OK;
   uint64_t cap = h->cfg.capacity ? h->cfg.capacity : std::max<uint64_t>(2 * n, 4096);
@@ -419,6 +447,10 @@ bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, 
   if (st) return st;
   st = upload(h->inst_slot_base, slot_base, h->stream);
   if (st) return st;
+  h->h_flags.assign(I, kInstActive);
+  h->h_target.assign(I, 0xFFFFFFFFu);
+  if ((st = upload(h->inst_flags, h->h_flags, h->stream)) || (st = upload(h->inst_target, h->h_target, h->stream)))
+    return st;
   BD_CUDA(h->zero_off.alloc((size_t)I * h->Z + 1));
   BD_CUDA(cudaMemsetAsync(h->zero_off.p, 0, ((size_t)I * h->Z + 1) * sizeof(uint32_t), h->stream));
   BD_CUDA(h->events.alloc((size_t)I * std::max(h->R, 1)));
@@ -473,6 +505,8 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->dtable.free();
   h->dgauss.free();
   h->inst_step.free();
+  h->inst_flags.free();
+  h->inst_target.free();
   h->inst_slot_base.free();
   h->zero_off.free();
   h->events.free();
@@ -535,68 +569,10 @@ BD_API bd_status bd_set_product_placement(bd_handle h, int rxn, int kind, float 
   return BD_OK;
 }
 
-BD_API bd_status bd_set_reaction_probability(bd_handle h, int rxn, float prob) {
-  if (!h || rxn < 0 || rxn >= (int)h->rx.size()) return BD_ERR_INVALID_ARGUMENT;
-  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
-  if (h->rx[rxn].order != 2 || !(prob >= 0.0f && prob <= 1.0f)) return BD_ERR_INVALID_ARGUMENT;
-  h->rx[rxn].user_prob = prob;
-  return BD_OK;
-}
-
-BD_API bd_status bd_finalize(bd_handle h) {
-  if (!h) return BD_ERR_INVALID_ARGUMENT;
-  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
-  if (h->D.empty()) return BD_ERR_INVALID_ARGUMENT;
-  if (!h->host_only) BD_CUDA(cudaSetDevice(h->device));
-  const int I = h->n_inst();
-  h->S = (int)h->D.size();
-  h->R = (int)h->rx.size();
-  bd_status first = BD_OK;
-  h->derived.clear();
-  for (int k = 0; k < I; k++) {
-    const bd_instance_desc& d = h->idesc[k];
-    const float vol = (d.box_hi[0] - d.box_lo[0]) * (d.box_hi[1] - d.box_lo[1]) * (d.box_hi[2] - d.box_lo[2]);
-    h->derived.push_back(derive_params(h->D, h->rx, h->cfg.dt, vol, d.d_scale, d.k2_scale));
-    if (!first && h->derived.back().status) {
-      first = h->derived.back().status;
-      g_last_error = h->derived.back().message;
-    }
-  }
-  // fatal setup errors leave the handle unfinalized
-  if (first == BD_ERR_NEGATIVE_RATE || first == BD_ERR_ZERO_DIFFUSION || first == BD_ERR_ILLEGAL_UNBIND) return first;
-
-  // network shape
-  h->uni_list.clear();
-  h->bim_list.clear();
-  h->zero_list.clear();
-  h->zero_two_products = false;
-  for (int s = 0; s < h->S; s++)
-    for (int r = 0; r < h->R; r++)
-      if (h->rx[r].order == 1 && h->rx[r].reactants[0] == s) h->uni_list.push_back(r);
-  for (int r = 0; r < h->R; r++) {
-    if (h->rx[r].order == 2) h->bim_list.push_back(r);
-    if (h->rx[r].order == 0) {
-      h->zero_list.push_back(r);
-      if (h->rx[r].nprod == 2) h->zero_two_products = true;
-    }
-  }
-  h->U = (int)h->uni_list.size();
-  h->B = (int)h->bim_list.size();
-  h->Z = (int)h->zero_list.size();
-  const int S = h->S, U = h->U, B = h->B, Z = h->Z;
-
-  // pair table: the last reaction listed for a pair wins (particleSystem.cpp:656-669);
-  // a reaction with zero binding radius never fires
-  h->bim_table.assign((size_t)S * S, -1);
-  for (int b = 0; b < B; b++) {
-    const ReactionDef& r = h->rx[h->bim_list[b]];
-    bool any = false;
-    for (int k = 0; k < I; k++) any |= h->derived[k].rx[h->bim_list[b]].bind_r2 > 0;
-    const int v = any ? b : -1;
-    h->bim_table[(size_t)r.reactants[0] * S + r.reactants[1]] = v;
-    h->bim_table[(size_t)r.reactants[1] * S + r.reactants[0]] = v;
-  }
-
+namespace {
+// Pack every instance's derived parameters into the device blocks.
+bd_status pack_blocks(bd_system* h) {
+  const int I = h->n_inst(), S = h->S, U = h->U, B = h->B, Z = h->Z;
   std::vector<DevSpecies> sp((size_t)I * S);
   std::vector<DevUni> un((size_t)I * U);
   std::vector<DevBim> bi((size_t)I * B);
@@ -654,10 +630,7 @@ BD_API bd_status bd_finalize(bd_handle h) {
       cdf.insert(cdf.end(), P.cdf[r].begin(), P.cdf[r].end());
     }
   }
-  if (h->host_only) {
-    h->finalized = true;
-    return first;
-  }
+  if (h->host_only) return BD_OK;
   std::vector<float> gauss(4096);
   gauss_quantiles(gauss.data(), 4096);
   bd_status st;
@@ -667,6 +640,72 @@ BD_API bd_status bd_finalize(bd_handle h) {
       (st = upload(h->dgauss, gauss, h->stream)))
     return st;
   BD_CUDA(cudaStreamSynchronize(h->stream));
+  return BD_OK;
+}
+}  // namespace
+
+BD_API bd_status bd_set_reaction_probability(bd_handle h, int rxn, float prob) {
+  if (!h || rxn < 0 || rxn >= (int)h->rx.size()) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (h->rx[rxn].order != 2 || !(prob >= 0.0f && prob <= 1.0f)) return BD_ERR_INVALID_ARGUMENT;
+  h->rx[rxn].user_prob = prob;
+  return BD_OK;
+}
+
+BD_API bd_status bd_finalize(bd_handle h) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (h->D.empty()) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->host_only) BD_CUDA(cudaSetDevice(h->device));
+  const int I = h->n_inst();
+  h->S = (int)h->D.size();
+  h->R = (int)h->rx.size();
+  bd_status first = BD_OK;
+  h->derived.clear();
+  for (int k = 0; k < I; k++) {
+    const bd_instance_desc& d = h->idesc[k];
+    const float vol = (d.box_hi[0] - d.box_lo[0]) * (d.box_hi[1] - d.box_lo[1]) * (d.box_hi[2] - d.box_lo[2]);
+    h->derived.push_back(derive_params(h->D, h->rx, h->cfg.dt, vol, d.d_scale, d.k2_scale));
+    if (!first && h->derived.back().status) {
+      first = h->derived.back().status;
+      g_last_error = h->derived.back().message;
+    }
+  }
+  // fatal setup errors leave the handle unfinalized
+  if (first == BD_ERR_NEGATIVE_RATE || first == BD_ERR_ZERO_DIFFUSION || first == BD_ERR_ILLEGAL_UNBIND) return first;
+
+  // network shape
+  h->uni_list.clear();
+  h->bim_list.clear();
+  h->zero_list.clear();
+  h->zero_two_products = false;
+  for (int s = 0; s < h->S; s++)
+    for (int r = 0; r < h->R; r++)
+      if (h->rx[r].order == 1 && h->rx[r].reactants[0] == s) h->uni_list.push_back(r);
+  for (int r = 0; r < h->R; r++) {
+    if (h->rx[r].order == 2) h->bim_list.push_back(r);
+    if (h->rx[r].order == 0) {
+      h->zero_list.push_back(r);
+      if (h->rx[r].nprod == 2) h->zero_two_products = true;
+    }
+  }
+  h->U = (int)h->uni_list.size();
+  h->B = (int)h->bim_list.size();
+  h->Z = (int)h->zero_list.size();
+  const int S = h->S, U = h->U, B = h->B, Z = h->Z;
+
+  // pair table: the last reaction listed for a pair wins (particleSystem.cpp:656-669);
+  // a reaction with zero binding radius never fires
+  h->bim_table.assign((size_t)S * S, -1);
+  for (int b = 0; b < B; b++) {
+    const ReactionDef& r = h->rx[h->bim_list[b]];
+    const int v = r.rate > 0 ? b : -1;
+    h->bim_table[(size_t)r.reactants[0] * S + r.reactants[1]] = v;
+    h->bim_table[(size_t)r.reactants[1] * S + r.reactants[0]] = v;
+  }
+
+  bd_status st = pack_blocks(h);
+  if (st) return st;
   h->finalized = true;
   return first;
 }
@@ -865,6 +904,217 @@ BD_API bd_status bd_get_state_pointer(bd_handle h, void** dev_records, uint64_t*
   if (st && st != BD_ERR_EMPTY) return st;
   *dev_records = h->hctrl->cur ? (void*)h->state1.p : (void*)h->state0.p;
   *n_slots = h->hctrl->n_slots;
+  return BD_OK;
+}
+
+// ------------------------------------------------------------------ serving
+
+BD_API bd_status bd_create_server(const bd_config* cfg, int max_instances, bd_handle* out) {
+  if (!cfg || max_instances < 1 || (uint32_t)max_instances > kMaxInstances) return BD_ERR_INVALID_ARGUMENT;
+  std::vector<bd_instance_desc> d(max_instances);
+  for (int k = 0; k < max_instances; k++) {
+    memset(&d[k], 0, sizeof(d[k]));
+    memcpy(d[k].box_lo, cfg->box_lo, sizeof(d[k].box_lo));
+    memcpy(d[k].box_hi, cfg->box_hi, sizeof(d[k].box_hi));
+    d[k].seed = cfg->seed + (uint64_t)k;
+    d[k].d_scale = d[k].k2_scale = 1.0f;
+  }
+  bd_status st = create_common(cfg, d.data(), max_instances, out);
+  if (st) return st;
+  bd_system* h = *out;
+  h->server = true;
+  h->slot_used.assign(max_instances, 0);
+  h->slot_free_after.assign(max_instances, UINT64_MAX);
+  return BD_OK;
+}
+
+namespace {
+
+// Slots whose instance was harvested become free once a step has dropped
+// its records.
+void release_slots(bd_system* h) {
+  for (int k = 0; k < h->n_inst(); k++)
+    if (h->slot_free_after[k] != UINT64_MAX && h->hctrl->step > h->slot_free_after[k]) {
+      h->slot_used[k] = 0;
+      h->slot_free_after[k] = UINT64_MAX;
+      h->h_flags[k] = 0;
+    }
+}
+
+template <class T>
+bd_status put1(DevBuf<T>& buf, int k, T v, cudaStream_t s) {
+  BD_CUDA(cudaMemcpyAsync(buf.p + k, &v, sizeof(T), cudaMemcpyHostToDevice, s));
+  BD_CUDA(cudaStreamSynchronize(s));
+  return BD_OK;
+}
+
+}  // namespace
+
+BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc* d, const float* xyz4, const int* species,
+                                   size_t n, uint32_t steps, int* slot_out) {
+  if (!h || !h->server || !d || !slot_out || steps == 0 || (n > 0 && (!xyz4 || !species)))
+    return BD_ERR_INVALID_ARGUMENT;
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  for (int a = 0; a < 3; a++)
+    if (!(d->box_hi[a] > d->box_lo[a])) return BD_ERR_INVALID_ARGUMENT;
+  BD_CUDA(cudaSetDevice(h->device));
+  const int I = h->n_inst();
+  bd_status st;
+  if (h->have_particles) {
+    st = bd_synchronize(h);
+    if (st && st != BD_ERR_EMPTY) return st;
+  }
+  if (h->h_flags.size() != (size_t)I) {
+    h->h_flags.assign(I, 0);
+    h->h_target.assign(I, 0xFFFFFFFFu);
+  }
+  release_slots(h);
+  int k = -1;
+  for (int j = 0; j < I && k < 0; j++)
+    if (!h->slot_used[j] && h->slot_free_after[j] == UINT64_MAX) k = j;
+  if (k < 0) return BD_ERR_CAPACITY;
+  bd_instance_desc dd = *d;
+  if (!(dd.d_scale > 0)) dd.d_scale = 1.0f;
+  if (!(dd.k2_scale > 0)) dd.k2_scale = 1.0f;
+  const float vol = (dd.box_hi[0] - dd.box_lo[0]) * (dd.box_hi[1] - dd.box_lo[1]) * (dd.box_hi[2] - dd.box_lo[2]);
+  DerivedParams P = derive_params(h->D, h->rx, h->cfg.dt, vol, dd.d_scale, dd.k2_scale);
+  if (P.status == BD_ERR_NEGATIVE_RATE || P.status == BD_ERR_ZERO_DIFFUSION || P.status == BD_ERR_ILLEGAL_UNBIND)
+    return P.status;
+  std::vector<float4> recs(n);
+  for (size_t i = 0; i < n; i++) {
+    const int s = species[i];
+    const float x = xyz4[4 * i], y = xyz4[4 * i + 1], z = xyz4[4 * i + 2];
+    if (s < 0 || s >= h->S || !(x >= dd.box_lo[0] && x <= dd.box_hi[0] && y >= dd.box_lo[1] && y <= dd.box_hi[1] &&
+                                z >= dd.box_lo[2] && z <= dd.box_hi[2]))
+      return BD_ERR_INVALID_ARGUMENT;
+    uint32_t w = ((uint32_t)k << 16) | (uint32_t)s;
+    float wf;
+    memcpy(&wf, &w, 4);
+    recs[i] = make_float4(x, y, z, wf);
+  }
+  h->idesc[k] = dd;
+  h->derived[k] = P;
+  if ((st = pack_blocks(h))) return st;
+  if (h->hinst.size() != (size_t)I) h->hinst.assign(I, DevInstance{});
+  h->slot_used[k] = 1;
+  plan_instance(h, k, n);
+  if ((st = layout_cells(h))) return st;
+  if (!h->have_particles) {
+    const uint64_t cap = std::max<uint64_t>(h->cfg.capacity, std::max<uint64_t>(2 * n, 1u << 20));
+    memset(h->hctrl, 0, sizeof(DevCtrl));
+    if ((st = grow_particles(h, cap))) return st;
+    const uint32_t pc = h->cfg.pair_capacity ? h->cfg.pair_capacity : (uint32_t)std::max<uint64_t>(65536, cap / 32);
+    if ((st = grow_pairs(h, pc))) return st;
+    std::vector<uint32_t> zeros(I, 0);
+    if ((st = upload(h->inst_step, zeros, h->stream)) || (st = upload(h->inst_slot_base, zeros, h->stream)) ||
+        (st = upload(h->inst_flags, h->h_flags, h->stream)) || (st = upload(h->inst_target, h->h_target, h->stream)))
+      return st;
+    BD_CUDA(h->zero_off.alloc((size_t)I * h->Z + 1));
+    BD_CUDA(cudaMemsetAsync(h->zero_off.p, 0, ((size_t)I * h->Z + 1) * sizeof(uint32_t), h->stream));
+    BD_CUDA(h->events.alloc((size_t)I * std::max(h->R, 1)));
+    BD_CUDA(h->pending.alloc((size_t)I * std::max(h->R, 1)));
+    BD_CUDA(cudaMemsetAsync(h->pending.p, 0, h->pending.n * sizeof(unsigned long long), h->stream));
+    h->have_particles = true;
+    h->target_step = 0;
+    if ((st = push_ctrl(h))) return st;
+  }
+  const uint64_t n_slots = h->hctrl->n_slots;
+  if (n_slots + n > h->capacity) {
+    if ((st = grow_particles(h, std::max<uint64_t>(2 * h->capacity, (n_slots + n) * 3 / 2)))) return st;
+    if ((st = push_ctrl(h))) return st;
+  }
+  float4* cur = h->hctrl->cur ? h->state1.p : h->state0.p;
+  if (n) BD_CUDA(cudaMemcpyAsync(cur + n_slots, recs.data(), n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  BD_CUDA(cudaMemsetAsync(h->events.p + (size_t)k * std::max(h->R, 1), 0,
+                          std::max(h->R, 1) * sizeof(unsigned long long), h->stream));
+  h->h_flags[k] = kInstActive;
+  h->h_target[k] = steps;
+  if ((st = put1(h->inst_step, k, 0u, h->stream)) || (st = put1(h->inst_slot_base, k, (uint32_t)n_slots, h->stream)) ||
+      (st = put1(h->inst_flags, k, (uint32_t)kInstActive, h->stream)) || (st = put1(h->inst_target, k, steps, h->stream)))
+    return st;
+  h->hctrl->n_slots = (uint32_t)(n_slots + n);
+  if ((st = push_ctrl(h))) return st;
+  if ((st = build_graphs(h))) return st;
+  *slot_out = k;
+  return BD_OK;
+}
+
+BD_API bd_status bd_instance_state(bd_handle h, int k, uint32_t* steps, uint32_t* flags) {
+  if (!h || !h->server || k < 0 || k >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->have_particles) {
+    if (steps) *steps = 0;
+    if (flags) *flags = 0;
+    return BD_OK;
+  }
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  uint32_t s = 0, f = 0;
+  BD_CUDA(cudaMemcpy(&s, h->inst_step.p + k, 4, cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(&f, h->inst_flags.p + k, 4, cudaMemcpyDeviceToHost));
+  if (steps) *steps = s;
+  if (flags) *flags = h->slot_used[k] ? f : 0;
+  return BD_OK;
+}
+
+BD_API bd_status bd_instance_poll(bd_handle h, int* slots, int cap, int* n_finished) {
+  if (!h || !h->server || !n_finished) return BD_ERR_INVALID_ARGUMENT;
+  *n_finished = 0;
+  if (!h->have_particles) return BD_OK;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const int I = h->n_inst();
+  std::vector<uint32_t> f(I);
+  BD_CUDA(cudaMemcpy(f.data(), h->inst_flags.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  int m = 0;
+  for (int k = 0; k < I; k++)
+    if (h->slot_used[k] && h->slot_free_after[k] == UINT64_MAX && (f[k] & kInstFrozen)) {
+      if (slots && m < cap) slots[m] = k;
+      m++;
+    }
+  *n_finished = m;
+  return BD_OK;
+}
+
+BD_API bd_status bd_instance_harvest(bd_handle h, int k, float* xyz4, int* species, size_t cap, size_t* n) {
+  if (!h || !h->server || !n || k < 0 || k >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  *n = 0;
+  if (!h->slot_used[k] || h->slot_free_after[k] != UINT64_MAX) return BD_ERR_INVALID_ARGUMENT;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const int I = h->n_inst();
+  std::vector<uint32_t> base(I), f(I);
+  BD_CUDA(cudaMemcpy(base.data(), h->inst_slot_base.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(f.data(), h->inst_flags.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  if (!(f[k] & kInstFrozen)) return BD_ERR_INVALID_ARGUMENT;
+  // the instance's records are contiguous: up to the next instance's first slot
+  uint64_t end = h->hctrl->n_slots;
+  for (int j = 0; j < I; j++)
+    if (j != k && h->slot_used[j] && base[j] > base[k] && base[j] < end) end = base[j];
+  const uint64_t len = end > base[k] ? end - base[k] : 0;
+  std::vector<float4> r(len);
+  const float4* cur = h->hctrl->cur ? h->state1.p : h->state0.p;
+  if (len) BD_CUDA(cudaMemcpy(r.data(), cur + base[k], len * sizeof(float4), cudaMemcpyDeviceToHost));
+  size_t m = 0;
+  for (const float4& q : r) {
+    uint32_t w;
+    memcpy(&w, &q.w, 4);
+    if (w == kDead || (int)(w >> 16) != k) continue;
+    if (m < cap) {
+      if (xyz4) {
+        xyz4[4 * m] = q.x;
+        xyz4[4 * m + 1] = q.y;
+        xyz4[4 * m + 2] = q.z;
+        xyz4[4 * m + 3] = 1.0f;
+      }
+      if (species) species[m] = (int)(w & 0xFFFFu);
+    }
+    m++;
+  }
+  *n = m;
+  h->h_flags[k] = f[k] | kInstRemoved;
+  if ((st = put1(h->inst_flags, k, h->h_flags[k], h->stream))) return st;
+  h->slot_free_after[k] = h->hctrl->step;
   return BD_OK;
 }
 

@@ -62,6 +62,21 @@ __device__ __forceinline__ float4* next_state(const KParams& p, uint32_t cur) {
   return cur ? p.state[0] : p.state[1];
 }
 
+// An instance advances when it is active, not frozen and not removed.
+__device__ __forceinline__ bool advancing(uint32_t flags) {
+  return (flags & kInstActive) && !(flags & (kInstFrozen | kInstRemoved));
+}
+
+// Commit one step of an instance; it freezes when it reaches its target, so
+// a request never runs past the step count it asked for.
+__device__ __forceinline__ void advance_instance_step(const KParams& p, uint32_t inst) {
+  const uint32_t f = p.inst_flags[inst];
+  if (!advancing(f)) return;
+  const uint32_t s = p.inst_step[inst] + 1;
+  p.inst_step[inst] = s;
+  if (s >= p.inst_target[inst]) p.inst_flags[inst] = f | kInstFrozen;
+}
+
 struct Out2 {
   float4 r[2];
   uint32_t key[2];
@@ -90,7 +105,7 @@ __device__ __forceinline__ void advance_real(const KParams& p, const float4* __r
   if (w == kDead) return;
   const uint32_t inst = w >> 16, sp = w & 0xFFFFu;
   const DevInstance& I = p.inst[inst];
-  const uint32_t flags = I.flags;
+  const uint32_t flags = p.inst_flags[inst];
   if (flags & kInstRemoved) return;
   if ((flags & kInstFrozen) || !(flags & kInstActive)) {
     o.r[0] = rec;
@@ -237,7 +252,7 @@ __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
     if (e < nz) {
       const uint32_t inst = e / p.Z, zr = e % p.Z;
       const DevInstance& I = p.inst[inst];
-      if ((I.flags & kInstActive) && !(I.flags & (kInstFrozen | kInstRemoved))) {
+      if (advancing(p.inst_flags[inst])) {
         const DevZero& Zr = p.zero[I.block * p.Z + zr];
         const U4 r = philox(U4{zr, p.inst_step[inst], kTagZeroCount, 0u}, I.key_lo, I.key_hi);
         const double u = u53_to_unit(r.x, r.y);
@@ -412,7 +427,7 @@ __global__ void __launch_bounds__(256) k_pairs(KParams p) {
     const uint32_t ci = s0 + canonical_rank(sc, s0, e0, i, r);
     nx[ci] = r;
     if (!kHasBim) continue;
-    if ((I.flags & (kInstFrozen | kInstRemoved)) || !(I.flags & kInstActive)) continue;
+    if (!advancing(p.inst_flags[inst])) continue;
     const DevSpecies S = p.species[I.block * p.S + sp];
     if (S.max_r <= 0.0f) continue;
 
@@ -587,7 +602,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
   commit_events(p);
   for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) {
     const DevInstance& I = p.inst[inst];
-    if ((I.flags & kInstActive) && !(I.flags & (kInstFrozen | kInstRemoved))) p.inst_step[inst] += 1;
+    advance_instance_step(p, inst);
     p.inst_slot_base[inst] = p.cell_start[I.cell_base];
   }
   if (threadIdx.x == 0) {
@@ -635,10 +650,7 @@ __global__ void k_finalize_inplace(KParams p) {
   DevCtrl* c = p.ctrl;
   if (ld_u32(&c->status)) return;
   commit_events(p);
-  for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) {
-    const DevInstance& I = p.inst[inst];
-    if ((I.flags & kInstActive) && !(I.flags & (kInstFrozen | kInstRemoved))) p.inst_step[inst] += 1;
-  }
+  for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) advance_instance_step(p, inst);
   if (threadIdx.x == 0) {
     c->n_slots += c->n_virtual;
     c->n_virtual = 0;

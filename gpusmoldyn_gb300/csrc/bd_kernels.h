@@ -21,6 +21,8 @@ struct KParams {
   const int32_t* bim_table;   // [S][S] -> local second-order index or -1
   const float* gauss;         // 4096 N(0,1) quantiles (table mode)
   uint32_t* inst_step;        // [I] steps taken by each instance
+  uint32_t* inst_flags;       // [I] InstanceFlags (frozen on device at the target)
+  const uint32_t* inst_target;// [I] step count at which an instance freezes
   uint32_t* inst_slot_base;   // [I] first slot of each instance in the current state
   uint32_t* zero_off;         // [I*Z + 1] prefix of zeroth-order births
   uint32_t* cell_count;       // [n_cells] particles per cell (returns to 0 each step)

@@ -22,6 +22,7 @@ class System:
     def __init__(self, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), dt=1e-3, seed=1, normals="boxmuller",
                  capacity=0, cell_size=0.0, cell_occupancy=0.0, pair_capacity=0, device=0, instances=None):
         self.lib = L.load()
+        self.server = False
         cfg = L.bd_config()
         self.lib.bd_config_default(C.byref(cfg))
         for a in range(3):
@@ -38,7 +39,14 @@ class System:
         self.cfg = cfg
         self.dt = dt
         self.h = C.c_void_p()
-        if instances is None:
+        if isinstance(instances, int):
+            # serving handle with `instances` slots filled by admit()
+            L.check(self.lib.bd_create_server(C.byref(cfg), instances, C.byref(self.h)), "bd_create_server")
+            self.server = True
+            self.n_instances = instances
+            self.instances = [dict(box_lo=tuple(box_lo), box_hi=tuple(box_hi), seed=seed + k, d_scale=1.0,
+                                   k2_scale=1.0, cell_size=0.0) for k in range(instances)]
+        elif instances is None:
             L.check(self.lib.bd_create(C.byref(cfg), C.byref(self.h)), "bd_create")
             self.n_instances = 1
             self.instances = [dict(box_lo=tuple(box_lo), box_hi=tuple(box_hi), seed=seed, d_scale=1.0,
@@ -201,6 +209,54 @@ class System:
         out = np.zeros(max(self.n_reactions, 1), np.uint64)
         L.check(self.lib.bd_get_event_counts(self.h, _ptr(out), self.n_reactions), "event_counts")
         return out[:self.n_reactions]
+
+    # ------------------------------------------------------------ serving
+    def admit(self, desc, pos, species, steps) -> int:
+        """Add a simulation to a serving handle; returns its slot."""
+        d = L.bd_instance_desc()
+        for a in range(3):
+            d.box_lo[a] = desc["box_lo"][a]
+            d.box_hi[a] = desc["box_hi"][a]
+        d.seed = desc.get("seed", 1)
+        d.d_scale = desc.get("d_scale", 1.0)
+        d.k2_scale = desc.get("k2_scale", 1.0)
+        d.cell_size = desc.get("cell_size", 0.0)
+        pos = np.asarray(pos, np.float32)
+        n = pos.shape[0]
+        p4 = np.zeros((max(n, 1), 4), np.float32)
+        p4[:n, :3] = pos[:, :3]
+        sp = np.ascontiguousarray(species, np.int32)
+        slot = C.c_int()
+        L.check(self.lib.bd_instance_admit(self.h, C.byref(d), _ptr(p4), _ptr(sp), n, int(steps), C.byref(slot)),
+                "bd_instance_admit")
+        self.instances[slot.value] = dict(desc)
+        return slot.value
+
+    def poll(self):
+        buf = np.zeros(max(self.n_instances, 1), np.int32)
+        m = C.c_int()
+        L.check(self.lib.bd_instance_poll(self.h, _ptr(buf), len(buf), C.byref(m)), "bd_instance_poll")
+        return [int(v) for v in buf[:m.value]]
+
+    def harvest(self, slot):
+        cap = 1 << 16
+        while True:
+            pos = np.zeros((cap, 4), np.float32)
+            sp = np.zeros(cap, np.int32)
+            n = C.c_size_t()
+            # harvest copies and frees in one call, so size the buffer first
+            steps, flags = self.instance_state(slot)
+            cnt = int(self.instance_counts()[slot])
+            if cnt > cap:
+                cap = cnt
+                continue
+            L.check(self.lib.bd_instance_harvest(self.h, slot, _ptr(pos), _ptr(sp), cap, C.byref(n)), "harvest")
+            return pos[:n.value, :3].copy(), sp[:n.value].copy()
+
+    def instance_state(self, slot):
+        s, f = C.c_uint32(), C.c_uint32()
+        L.check(self.lib.bd_instance_state(self.h, slot, C.byref(s), C.byref(f)), "bd_instance_state")
+        return s.value, f.value
 
     def time_steps(self, n) -> float:
         """Device time in ms of n steps (CUDA events on the handle's stream)."""

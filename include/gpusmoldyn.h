@@ -274,6 +274,23 @@ BD_API bd_status bd_get_instance_particles(bd_handle h, int instance, float *xyz
 BD_API bd_status bd_get_instance_reaction_info(bd_handle h, int instance, int rxn,
                                                bd_reaction_info *out);
 
+/* -------------------------------------------------------------- serving */
+/* A serving handle: an ensemble of max_instances slots that are filled and
+ * emptied while it runs (continuous batching).  Species and reactions are
+ * added and finalized as usual; then bd_instance_admit adds a simulation,
+ * bd_step advances every admitted instance together, an instance freezes on
+ * the device when it reaches its step count, bd_instance_poll lists frozen
+ * instances and bd_instance_harvest copies one out and frees its slot.  An
+ * instance evolves exactly as it would alone.  The reference runs one
+ * system per process and has no counterpart. */
+BD_API bd_status bd_create_server(const bd_config *cfg, int max_instances, bd_handle *out);
+BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc *d, const float *xyz4, const int *species,
+                                   size_t n, uint32_t steps, int *slot);
+BD_API bd_status bd_instance_poll(bd_handle h, int *slots, int cap, int *n_finished);
+BD_API bd_status bd_instance_harvest(bd_handle h, int slot, float *xyz4, int *species, size_t cap, size_t *n);
+/* Steps taken by the instance in a slot and its flags (1 active, 2 frozen). */
+BD_API bd_status bd_instance_state(bd_handle h, int slot, uint32_t *steps, uint32_t *flags);
+
 /* ------------------------------------------------------ rxnparam (host) */
 /* Restatements of rxnparam.h:39-42 (Andrews-Bray rate tables, rxnparam.cpp:
  * 42-308): rate per step in length^3, binding radius, unbinding radius. */

@@ -78,7 +78,7 @@ def test_irreversible_c1_shape_bit_exact():
 
 def test_contested_pairs_bit_exact():
     # dense enough that particles have several partners: the matching matters
-    s = dense_a_b(3000, 3000, 1.2, seed=12, kon=40.0)
+    s = dense_a_b(3000, 3000, 1.2, seed=12, kon=4.0)
     o = orc.OracleSystem(s)
     recs = gpu_records(s)
     res = o.step(0, recs, want_pairs=True)
@@ -198,8 +198,8 @@ def test_capacity_growth_replays_exactly():
 
 
 def test_pair_capacity_growth_replays_exactly():
-    a = dense_a_b(3000, 3000, 1.2, seed=19, kon=40.0, pair_capacity=8)
-    b = dense_a_b(3000, 3000, 1.2, seed=19, kon=40.0)
+    a = dense_a_b(3000, 3000, 1.2, seed=19, kon=4.0, pair_capacity=8)
+    b = dense_a_b(3000, 3000, 1.2, seed=19, kon=4.0)
     for s in (a, b):
         s.step(5)
         s.synchronize()

@@ -1,0 +1,98 @@
+"""Continuous batching: simulations admitted into a running serving handle
+give the same result as when each runs alone, bit for bit, and stop exactly
+at their requested step count."""
+import numpy as np
+import pytest
+
+from gpusmoldyn_gb300 import _lib as L
+from gpusmoldyn_gb300.configs import rng, uniform_positions
+from gpusmoldyn_gb300.system import System
+
+pytestmark = pytest.mark.gpu
+
+
+def network(s):
+    A, B, Cc = s.add_species(1.0), s.add_species(1.0), s.add_species(0.5)
+    s.add_reaction(2, [A, B], [Cc], 2.0)
+    back = s.add_reaction(1, [Cc], [A, B], 40.0)
+    s.set_product_placement(back, L.BD_PP_UNBINDRAD, 0.01)
+    s.add_reaction(0, [], [A], 300.0)
+    s.finalize()
+
+
+def job(k):
+    n = [3000, 12000, 700, 6000][k]
+    side = float((n / 2000.0) ** (1 / 3))
+    desc = dict(box_lo=(0.0, 0.0, 0.0), box_hi=(side, side, side), seed=77 + k, d_scale=[1.0, 0.7, 1.4, 1.1][k],
+                k2_scale=[1.0, 2.0, 0.5, 1.5][k])
+    g = rng(500 + k)
+    pos = uniform_positions(g, n, desc["box_lo"], desc["box_hi"])
+    sp = (np.arange(n) % 2).astype(np.int32)
+    return desc, pos, sp, [30, 55, 80, 41][k]
+
+
+def run_until_frozen(s, slot, chunk=7):
+    while True:
+        if slot in s.poll():
+            return s.harvest(slot)
+        s.step(chunk)
+        s.synchronize()
+
+
+def test_same_alone_and_in_the_mix():
+    alone = {}
+    for k in range(4):
+        s = System(dt=1e-3, instances=1)
+        network(s)
+        desc, pos, sp, steps = job(k)
+        slot = s.admit(desc, pos, sp, steps)
+        alone[k] = run_until_frozen(s, slot)
+        s.close()
+
+    mix = System(dt=1e-3, instances=3)
+    network(mix)
+    results, slots, admitted = {}, {}, []
+    pending = [0, 1, 2, 3]
+    t = 0
+    while pending or slots:
+        # admit as slots free up, at staggered times
+        if pending and len(slots) < 3 and t % 9 == 0:
+            k = pending.pop(0)
+            desc, pos, sp, steps = job(k)
+            slots[mix.admit(desc, pos, sp, steps)] = k
+        mix.step(3)
+        t += 3
+        for slot in mix.poll():
+            steps_done, flags = mix.instance_state(slot)
+            k = slots.pop(slot)
+            assert steps_done == job(k)[3] and flags & 2
+            results[k] = mix.harvest(slot)
+    mix.close()
+    for k in range(4):
+        pa, sa = alone[k]
+        pm, sm = results[k]
+        assert pa.shape == pm.shape and len(pa) > 0
+        np.testing.assert_array_equal(pa, pm, err_msg=f"job {k}")
+        np.testing.assert_array_equal(sa, sm, err_msg=f"job {k}")
+
+
+def test_server_slots_are_reused():
+    s = System(dt=1e-3, instances=2)
+    network(s)
+    for rnd in range(3):
+        got = []
+        for k in (0, 2):
+            desc, pos, sp, _ = job(k)
+            got.append(s.admit(desc, pos, sp, 5))
+        assert sorted(got) == [0, 1]
+        done = []
+        while len(done) < 2:
+            s.step(2)
+            s.synchronize()
+            for slot in s.poll():
+                done.append(slot)
+                p, q = s.harvest(slot)
+                assert len(p) > 0
+        s.step(1)  # drops the harvested records, frees the slots
+        s.synchronize()
+    s.close()
