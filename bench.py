@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--serve-jobs", type=int, default=40)
     p.add_argument("--profile-only", action="store_true", help="build + a few steps (for ncu)")
     return p.parse_args()
 
@@ -369,6 +371,10 @@ def run_gb300(args, dist):
     if not args.no_batched:
         out["batched"] = run_batched(args, dist, device)
 
+    # ---------------- serving: continuous batching of c5-style requests
+    if not args.no_serving and dist.rank == 0:
+        out["serving"] = run_serving(args, device)
+
     # ---------------- CPU baseline (rank 0, N = 1 only)
     if not args.no_cpu and dist.rank == 0 and dist.world == 1:
         threads = os.cpu_count() or 1
@@ -412,6 +418,22 @@ def run_batched(args, dist, device):
     return {"workload": f"c4: {len(inst)} instances of the c2 network, {int(np.sum(counts))} particles",
             "value": batched, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
             "plain_loop_value": loop, "speedup_vs_plain_loop": batched / loop}
+
+
+def run_serving(args, device):
+    """c5: Poisson arrivals at 50/s of c3-network simulations with N
+    log-uniform in 1e3-5e6 and steps uniform in 100-10000, admitted into one
+    serving handle against a 150 GB budget."""
+    from gpusmoldyn_gb300 import configs
+    from gpusmoldyn_gb300.serve import Server
+
+    jobs = configs.c5_jobs(args.serve_jobs, seed=5)
+    srv = Server(max_instances=64, hbm_budget=150e9, chunk=10, device=device)
+    res = srv.run(jobs)
+    srv.close()
+    return {"workload": f"c5: {len(jobs)} requests, Poisson 50/s, N log-U[1e3, 5e6], steps U[100, 10000]",
+            "p50_latency_s": res["p50_s"], "p99_latency_s": res["p99_s"], "mean_latency_s": res["mean_s"],
+            "value": res["particle_steps_per_s"], "unit": UNIT, "wall_s": res["wall_s"], "jobs": res["jobs"]}
 
 
 def main():

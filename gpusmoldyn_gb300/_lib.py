@@ -101,6 +101,7 @@ _SIGS = {
                                      C.POINTER(C.c_size_t)]),
     "bd_get_species_d": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "bd_set_cell_size": (C.c_int, [H, C.c_float]),
+    "bd_set_launch_shape": (C.c_int, [H, C.c_int, C.c_int, C.c_int, C.c_int]),
     "bd_create_server": (C.c_int, [C.POINTER(bd_config), C.c_int, C.POINTER(H)]),
     "bd_instance_admit": (C.c_int, [H, C.POINTER(bd_instance_desc), P, P, C.c_size_t, C.c_uint32,
                                     C.POINTER(C.c_int)]),

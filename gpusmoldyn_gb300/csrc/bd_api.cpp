@@ -1353,6 +1353,21 @@ BD_API bd_status bd_get_species_d(bd_handle h, int inst, int species, float* D) 
   return BD_OK;
 }
 
+BD_API bd_status bd_set_launch_shape(bd_handle h, int bs, int cs, int bp, int cp) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  for (int b : {bs, bp})
+    if (b < 32 || b > 256 || b % 32) return BD_ERR_INVALID_ARGUMENT;
+  if (cs < 1 || cs > 64 || cp < 1 || cp > 64) return BD_ERR_INVALID_ARGUMENT;
+  h->shape.block_stream = bs;
+  h->shape.grid_stream = h->n_sm * cs;
+  h->shape.block_pairs = bp;
+  h->shape.grid_pairs = h->n_sm * cp;
+  if (h->host_only || !h->have_particles) return BD_OK;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  return build_graphs(h);
+}
+
 BD_API bd_status bd_set_cell_size(bd_handle h, float cell_size) {
   if (!h || !(cell_size >= 0)) return BD_ERR_INVALID_ARGUMENT;
   h->cell_override = cell_size;

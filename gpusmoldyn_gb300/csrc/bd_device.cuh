@@ -28,9 +28,10 @@ struct U4 {
 __device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
-    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    // one 32x32->64 multiply each (IMAD.WIDE) gives both halves
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+    c = U4{(uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0};
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
   }
@@ -67,13 +68,16 @@ __device__ __forceinline__ void normals3(const U4& r, const float* __restrict__ 
     g1 = table[r.y >> 20];
     g2 = table[r.z >> 20];
   } else {
+    // hardware approximations (MUFU lg2 / rsqrt / sin / cos): absolute
+    // errors ~1e-6, far below the statistical resolution of the step
     const float a = u24_to_unit(r.x) + 2.98023223876953125e-08f;  // (0, 1)
     const float c = u24_to_unit(r.z) + 2.98023223876953125e-08f;
-    const float ra = sqrtf(-2.0f * logf(a));
-    const float rc = sqrtf(-2.0f * logf(c));
+    const float la = -2.0f * __logf(a), lc = -2.0f * __logf(c);  // > 0
+    const float ra = la * rsqrtf(la);
+    const float rc = lc * rsqrtf(lc);
     float sa, ca, sc, cc;
-    sincospif(2.0f * u24_to_unit(r.y), &sa, &ca);
-    sincospif(2.0f * u24_to_unit(r.w), &sc, &cc);
+    __sincosf(6.2831853071795865f * u24_to_unit(r.y), &sa, &ca);
+    __sincosf(6.2831853071795865f * u24_to_unit(r.w), &sc, &cc);
     g0 = ra * ca;
     g1 = ra * sa;
     g2 = rc * cc;

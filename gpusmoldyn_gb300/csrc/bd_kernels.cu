@@ -103,7 +103,7 @@ __device__ __forceinline__ void advance_real(const KParams& p, const float4* __r
   const float4 rec = cur[i];
   const uint32_t w = rec_w(rec);
   if (w == kDead) return;
-  const uint32_t inst = w >> 16, sp = w & 0xFFFFu;
+  const uint32_t inst = w >> 16, sp = w & kSpeciesMask;
   const DevInstance& I = p.inst[inst];
   const uint32_t flags = p.inst_flags[inst];
   if (flags & kInstRemoved) return;
@@ -147,7 +147,7 @@ __device__ __forceinline__ void advance_real(const KParams& p, const float4* __r
           y = reflect(__fmaf_rn(u.off0, dy, y), I.lo[1], I.hi[1]);
           z = reflect(__fmaf_rn(u.off0, dz, z), I.lo[2], I.hi[2]);
         }
-        o.r[1] = make_float4(bx, by, bz, __uint_as_float(pack_w(inst, (uint32_t)u.prod1)));
+        o.r[1] = make_float4(bx, by, bz, __uint_as_float(pack_w(inst, (uint32_t)u.prod1) | kNewborn));
         o.key[1] = cell_key(I, bx, by, bz);
         n = 2;
       }
@@ -180,11 +180,11 @@ __device__ __forceinline__ void advance_virtual(const KParams& p, uint32_t v, Ou
   const float z = fminf(__fmaf_rn(u24_to_unit(r.z), __fsub_rn(I.hi[2], I.lo[2]), I.lo[2]), I.hi[2]);
   const DevZero& Zr = p.zero[I.block * p.Z + zr];
   const uint32_t key = cell_key(I, x, y, z);
-  o.r[0] = make_float4(x, y, z, __uint_as_float(pack_w(inst, (uint32_t)Zr.prod0)));
+  o.r[0] = make_float4(x, y, z, __uint_as_float(pack_w(inst, (uint32_t)Zr.prod0) | kNewborn));
   o.key[0] = key;
   o.n = 1;
   if (Zr.prod1 >= 0) {
-    o.r[1] = make_float4(x, y, z, __uint_as_float(pack_w(inst, (uint32_t)Zr.prod1)));
+    o.r[1] = make_float4(x, y, z, __uint_as_float(pack_w(inst, (uint32_t)Zr.prod1) | kNewborn));
     o.key[1] = key;
     o.n = 2;
   }
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(256) k_count(KParams p) {
     if (i < n_real) advance_real<kTable, true>(p, st, i, o);
     else if (i < n_total) advance_virtual(p, i - n_real, o);
     warp_count(p.cell_count, o.n > 0 ? o.key[0] : kNoKey);
-    warp_count(p.cell_count, o.n > 1 ? o.key[1] : kNoKey);
+    if (__any_sync(kFull, o.n > 1)) warp_count(p.cell_count, o.n > 1 ? o.key[1] : kNoKey);
   }
 }
 
@@ -371,8 +371,10 @@ __global__ void __launch_bounds__(256) k_scatter(KParams p) {
     o.n = 0;
     if (i < n_real) advance_real<kTable, false>(p, st, i, o);
     else if (i < n_total) advance_virtual(p, i - n_real, o);
+    const int kmax = __any_sync(kFull, o.n > 1) ? 2 : 1;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
+      if (k >= kmax) break;  // warp-uniform
       const uint32_t key = o.n > k ? o.key[k] : kNoKey;
       const uint32_t off = warp_claim(p.cell_count, key);
       if (key != kNoKey) {
@@ -413,63 +415,75 @@ __global__ void __launch_bounds__(256) k_pairs(KParams p) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const float4 r = sc[i];
     const uint32_t w = rec_w(r);
-    const uint32_t inst = w >> 16, sp = w & 0xFFFFu;
-    const DevInstance& I = p.inst[inst];
-    const int cx = cell_coord(r.x, I.lo[0], I.inv[0], I.dims[0]);
-    const int cy = cell_coord(r.y, I.lo[1], I.inv[1], I.dims[1]);
-    const int cz = cell_coord(r.z, I.lo[2], I.inv[2], I.dims[2]);
-    const uint32_t key = I.cell_base + ((uint32_t)cz * I.dims[1] + (uint32_t)cy) * I.dims[0] + (uint32_t)cx;
-    const uint32_t s0 = p.cell_start[key], e0 = p.cell_start[key + 1];
+    const uint32_t inst = w >> 16, sp = w & kSpeciesMask;
+    const DevInstance* __restrict__ Ip = p.inst + inst;
+    // the instance's grid in registers (no reloads across the stores below)
+    const float lo0 = __ldg(&Ip->lo[0]), lo1 = __ldg(&Ip->lo[1]), lo2 = __ldg(&Ip->lo[2]);
+    const float iv0 = __ldg(&Ip->inv[0]), iv1 = __ldg(&Ip->inv[1]), iv2 = __ldg(&Ip->inv[2]);
+    const uint32_t d0 = __ldg(&Ip->dims[0]), d1 = __ldg(&Ip->dims[1]), d2 = __ldg(&Ip->dims[2]);
+    const uint32_t cbase = __ldg(&Ip->cell_base);
+    const int cx = cell_coord(r.x, lo0, iv0, d0);
+    const int cy = cell_coord(r.y, lo1, iv1, d1);
+    const int cz = cell_coord(r.z, lo2, iv2, d2);
+    const uint32_t key = cbase + ((uint32_t)cz * d1 + (uint32_t)cy) * d0 + (uint32_t)cx;
+    const uint32_t s0 = __ldg(&p.cell_start[key]), e0 = __ldg(&p.cell_start[key + 1]);
     if (i < s0 || i >= e0) {
       atomicOr(&c->status, kStatBounds);
       continue;
     }
     const uint32_t ci = s0 + canonical_rank(sc, s0, e0, i, r);
-    nx[ci] = r;
-    if (!kHasBim) continue;
-    if (!advancing(p.inst_flags[inst])) continue;
-    const DevSpecies S = p.species[I.block * p.S + sp];
-    if (S.max_r <= 0.0f) continue;
+    // the newborn mark lives only within this step
+    nx[ci] = make_float4(r.x, r.y, r.z, __uint_as_float(w & ~kNewborn));
+    if (!kHasBim || (w & kNewborn)) continue;
+    if (!advancing(__ldg(&p.inst_flags[inst]))) continue;
+    const uint32_t block = __ldg(&Ip->block);
+    const float max_r = __ldg(&p.species[block * p.S + sp].max_r);
+    if (max_r <= 0.0f) continue;
+    const float cl0 = __ldg(&Ip->cell[0]), cl1 = __ldg(&Ip->cell[1]), cl2 = __ldg(&Ip->cell[2]);
 
     // distances to the six faces of the cell, for pruning neighbour cells
-    const float fx = __fsub_rn(__fmul_rn(__fsub_rn(r.x, I.lo[0]), I.inv[0]), (float)cx);
-    const float fy = __fsub_rn(__fmul_rn(__fsub_rn(r.y, I.lo[1]), I.inv[1]), (float)cy);
-    const float fz = __fsub_rn(__fmul_rn(__fsub_rn(r.z, I.lo[2]), I.inv[2]), (float)cz);
-    const float lox = fx * I.cell[0], hix = (1.0f - fx) * I.cell[0];
-    const float loy = fy * I.cell[1], hiy = (1.0f - fy) * I.cell[1];
-    const float loz = fz * I.cell[2], hiz = (1.0f - fz) * I.cell[2];
-    const float need = S.max_r + p.prune_margin * fminf(I.cell[0], fminf(I.cell[1], I.cell[2]));
+    const float fx = __fsub_rn(__fmul_rn(__fsub_rn(r.x, lo0), iv0), (float)cx);
+    const float fy = __fsub_rn(__fmul_rn(__fsub_rn(r.y, lo1), iv1), (float)cy);
+    const float fz = __fsub_rn(__fmul_rn(__fsub_rn(r.z, lo2), iv2), (float)cz);
+    const float lox = fx * cl0, hix = (1.0f - fx) * cl0;
+    const float loy = fy * cl1, hiy = (1.0f - fy) * cl1;
+    const float loz = fz * cl2, hiz = (1.0f - fz) * cl2;
+    const float need = max_r + p.prune_margin * fminf(cl0, fminf(cl1, cl2));
     const float need2 = need * need;
-    const uint32_t base_new = p.cell_start[I.cell_base];
-    const uint32_t t = p.inst_step[inst];
     const int32_t* __restrict__ row = p.bim_table + sp * p.S;
 
-    for (int dz = -1; dz <= 1; ++dz) {
+    // only the neighbours across faces closer than the largest binding
+    // radius can hold a partner: usually the particle's own cell alone
+    const int zlo = (cz > 0 && loz <= need) ? -1 : 0, zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
+    const int ylo = (cy > 0 && loy <= need) ? -1 : 0, yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
+    const int xlo = (cx > 0 && lox <= need) ? -1 : 0, xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
       const int nz_ = cz + dz;
-      if (nz_ < 0 || nz_ >= (int)I.dims[2]) continue;
       const float ddz = dz < 0 ? loz : (dz > 0 ? hiz : 0.0f);
-      for (int dy = -1; dy <= 1; ++dy) {
+      for (int dy = ylo; dy <= yhi; ++dy) {
         const int ny_ = cy + dy;
-        if (ny_ < 0 || ny_ >= (int)I.dims[1]) continue;
         const float ddy = dy < 0 ? loy : (dy > 0 ? hiy : 0.0f);
-        for (int dx = -1; dx <= 1; ++dx) {
+        for (int dx = xlo; dx <= xhi; ++dx) {
           const int nx_ = cx + dx;
-          if (nx_ < 0 || nx_ >= (int)I.dims[0]) continue;
           const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
           if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
-          const uint32_t nkey = I.cell_base + ((uint32_t)nz_ * I.dims[1] + (uint32_t)ny_) * I.dims[0] + (uint32_t)nx_;
-          const uint32_t ns = p.cell_start[nkey], ne = p.cell_start[nkey + 1];
+          const uint32_t nkey = cbase + ((uint32_t)nz_ * d1 + (uint32_t)ny_) * d0 + (uint32_t)nx_;
+          const uint32_t ns = __ldg(&p.cell_start[nkey]), ne = __ldg(&p.cell_start[nkey + 1]);
           for (uint32_t m = ns; m < ne; ++m) {
             if (m == i) continue;
             const float4 q = sc[m];
-            const int32_t b = row[rec_w(q) & 0xFFFFu];
+            const uint32_t wq = rec_w(q);
+            if (wq & kNewborn) continue;
+            const int32_t b = __ldg(&row[wq & kSpeciesMask]);
             if (b < 0) continue;
-            const DevBim& br = p.bim[I.block * p.B + (uint32_t)b];
-            if (dist2(r, q) > br.r2) continue;
+            const DevBim& br = p.bim[block * p.B + (uint32_t)b];
+            if (dist2(r, q) > __ldg(&br.r2)) continue;
             const uint32_t cj = ns + canonical_rank(sc, ns, ne, m, q);
             if (ci >= cj) continue;  // the pair is reported by its lower slot
-            if (br.prob < 1.0f) {
-              const U4 u = philox(U4{ci - base_new, t, kTagBimCoin, cj - base_new}, I.key_lo, I.key_hi);
+            if (__ldg(&br.prob) < 1.0f) {
+              const uint32_t base_new = __ldg(&p.cell_start[cbase]);
+              const U4 u = philox(U4{ci - base_new, __ldg(&p.inst_step[inst]), kTagBimCoin, cj - base_new},
+                                  __ldg(&Ip->key_lo), __ldg(&Ip->key_hi));
               if (!(u32_to_unit(u.x) < br.prob)) continue;
             }
             const uint32_t idx = atomicAdd(&c->n_pairs, 1u);
@@ -558,7 +572,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     const DevInstance& I = p.inst[inst];
     const DevBim br = p.bim[I.block * p.B + b];
     const float4 ri = nx[q.i], rj = nx[q.j];
-    const bool i_first = (int32_t)(rec_w(ri) & 0xFFFFu) == br.react0;
+    const bool i_first = (int32_t)(rec_w(ri) & kSpeciesMask) == br.react0;
     const uint32_t m1 = i_first ? q.i : q.j, m2 = i_first ? q.j : q.i;
     const float4 p1 = i_first ? ri : rj, p2 = i_first ? rj : ri;
     const float rx = __fmaf_rn(br.x, p1.x, __fmul_rn(br.omx, p2.x));
@@ -642,7 +656,7 @@ __global__ void __launch_bounds__(256) k_append(KParams p) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += stride) {
     Out2 o;
     advance_virtual(p, v, o);
-    st[n + v] = o.r[0];
+    st[n + v] = make_float4(o.r[0].x, o.r[0].y, o.r[0].z, __uint_as_float(rec_w(o.r[0]) & ~kNewborn));
   }
 }
 
@@ -691,7 +705,7 @@ __global__ void __launch_bounds__(256) k_species_counts(KParams p, unsigned long
     uint32_t key = kNoKey;
     if (i < n) {
       const uint32_t w = rec_w(st[i]);
-      if (w != kDead) key = (w >> 16) * p.S + (w & 0xFFFFu);
+      if (w != kDead) key = (w >> 16) * p.S + (w & kSpeciesMask);
     }
     const uint32_t peers = __match_any_sync(kFull, key);
     if (key != kNoKey && lane_id() == (uint32_t)(__ffs(peers) - 1))

@@ -2,7 +2,7 @@
 // the host packer (bd_api.cpp) and the kernels (bd_kernels.cu).
 //
 // Particle record: one float4 per slot, x, y, z and a 32-bit word w holding
-// species (bits 0-15) and instance (bits 16-31); w = 0xFFFFFFFF marks an empty
+// species (bits 0-14) and instance (bits 16-31); w = 0xFFFFFFFF marks an empty
 // slot (a particle that died in the bimolecular phase).  The reference keeps
 // positions (float4, w = radius/flag) and types (int) in two arrays
 // (particleSystem.h:151-152, 204-205); one 16-byte record halves the number
@@ -21,7 +21,14 @@
 namespace bd {
 
 constexpr uint32_t kDead = 0xFFFFFFFFu;
-constexpr uint32_t kMaxSpecies = 0xFFFEu;
+// Bit 15 of w marks a particle born in the step in flight (second product
+// of a first-order reaction, zeroth-order birth).  It exists only between
+// the scatter and the pair kernel: newborns are sorted into their cells but
+// take no part in that step's bimolecular search, as the reference appends
+// them only after collide (particleSystem.cpp:984-991).
+constexpr uint32_t kNewborn = 0x8000u;
+constexpr uint32_t kSpeciesMask = 0x7FFFu;
+constexpr uint32_t kMaxSpecies = 0x7FFEu;
 constexpr uint32_t kMaxInstances = 0xFFFFu;
 
 // Philox counter word 2 carries a stream tag in its top byte.

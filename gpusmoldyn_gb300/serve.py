@@ -1,0 +1,112 @@
+"""Continuous-batching request loop over a serving handle.
+
+Requests (simulations with their own size, seed and step count) arrive over
+time.  Each loop iteration admits the requests that have arrived while a
+slot and the HBM budget allow, advances every admitted simulation together
+by a chunk of steps (one pipeline over all of them, one graph launch per
+step), then harvests the simulations that reached their step count.  A
+simulation freezes on the device at exactly its step count, so chunking
+never overshoots, and it evolves bit for bit as it would alone.
+"""
+from __future__ import annotations
+
+import collections
+import math
+import time
+
+import numpy as np
+
+from .configs import c3_network, c3_zeroth_rate, rng, uniform_positions
+from .system import System
+
+# device bytes per particle slot: two state buffers + the sort staging buffer
+# (16 B each) + the matcher word (4 B), with 2x headroom for growth
+BYTES_PER_PARTICLE = 2 * (16 * 3 + 4)
+
+
+def c3_request(job, density=2.0):
+    """Initial state of one c3-style request: n particles of the 8-species
+    network at the c3 density in a cube sized for them."""
+    n = job["n"]
+    side = float((n / density) ** (1.0 / 3.0))
+    desc = dict(box_lo=(0.0, 0.0, 0.0), box_hi=(side, side, side), seed=job["seed"])
+    g = rng(job["seed"])
+    pos = uniform_positions(g, n, desc["box_lo"], desc["box_hi"])
+    sp = (np.arange(n) % 8).astype(np.int32)
+    return desc, pos, sp, job["steps"]
+
+
+def c3_server_network(s, density=2.0, network_seed=3):
+    D, rx = c3_network(network_seed)
+    for d in D:
+        s.add_species(float(d))
+    z = c3_zeroth_rate(D, rx, density)
+    s.add_reaction(0, [], [0], z)
+    s.add_reaction(0, [], [1], z)
+    for order, rc, pr, k in rx:
+        s.add_reaction(order, rc, pr, float(k))
+    s.finalize()
+
+
+class Server:
+    def __init__(self, network=c3_server_network, max_instances=64, hbm_budget=150e9, dt=1e-3, chunk=10,
+                 device=0, normals="boxmuller"):
+        self.s = System(dt=dt, instances=max_instances, device=device, normals=normals)
+        network(self.s)
+        self.max_instances = max_instances
+        self.budget = hbm_budget
+        self.chunk = chunk
+
+    def run(self, jobs, make_request=c3_request, time_scale=1.0, keep_results=False):
+        """Serve `jobs` (dicts with arrival [s], n, steps, seed); returns
+        per-job latencies and throughput figures."""
+        s = self.s
+        pending = collections.deque(sorted(jobs, key=lambda j: j["arrival"]))
+        waiting = collections.deque()
+        active = {}  # slot -> (job, bytes)
+        used = 0.0
+        done = []
+        psteps = 0.0
+        t0 = time.perf_counter()
+        while pending or waiting or active:
+            now = time.perf_counter() - t0
+            while pending and pending[0]["arrival"] * time_scale <= now:
+                waiting.append(pending.popleft())
+            while waiting and len(active) < self.max_instances:
+                job = waiting[0]
+                need = job["n"] * BYTES_PER_PARTICLE
+                if used + need > self.budget and active:
+                    break
+                waiting.popleft()
+                desc, pos, sp, steps = make_request(job)
+                slot = s.admit(desc, pos, sp, steps)
+                job["admitted"] = time.perf_counter() - t0
+                active[slot] = (job, need)
+                used += need
+            if not active:
+                if pending:
+                    time.sleep(max(0.0, pending[0]["arrival"] * time_scale - (time.perf_counter() - t0)))
+                continue
+            live = sum(j["n"] for j, _ in active.values())
+            s.step(self.chunk)
+            s.synchronize()
+            psteps += live * self.chunk
+            for slot in s.poll():
+                job, need = active.pop(slot)
+                pos, sp = s.harvest(slot)
+                job["finished"] = time.perf_counter() - t0
+                job["latency"] = job["finished"] - job["arrival"] * time_scale
+                job["n_final"] = int(len(sp))
+                if keep_results:
+                    job["result"] = (pos, sp)
+                used -= need
+                done.append(job)
+        wall = time.perf_counter() - t0
+        lat = np.array([j["latency"] for j in done])
+        work = float(sum(j["n"] * j["steps"] for j in done))
+        return dict(jobs=len(done), wall_s=wall, p50_s=float(np.percentile(lat, 50)),
+                    p99_s=float(np.percentile(lat, 99)), mean_s=float(lat.mean()),
+                    particle_steps_per_s=work / wall, approx_device_particle_steps=psteps, done=done)
+
+    def close(self):
+        self.s.close()

@@ -258,6 +258,10 @@ class System:
         L.check(self.lib.bd_instance_state(self.h, slot, C.byref(s), C.byref(f)), "bd_instance_state")
         return s.value, f.value
 
+    def set_launch_shape(self, block_stream=256, ctas_stream=8, block_pairs=256, ctas_pairs=8):
+        L.check(self.lib.bd_set_launch_shape(self.h, block_stream, ctas_stream, block_pairs, ctas_pairs),
+                "bd_set_launch_shape")
+
     def time_steps(self, n) -> float:
         """Device time in ms of n steps (CUDA events on the handle's stream)."""
         ms = C.c_float()

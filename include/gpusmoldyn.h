@@ -237,6 +237,12 @@ BD_API bd_status bd_get_poisson_cdf(bd_handle h, int instance, int rxn, double *
 BD_API bd_status bd_get_species_d(bd_handle h, int instance, int species, float *D);
 /* Cell edge override before the first step (autotuner). */
 BD_API bd_status bd_set_cell_size(bd_handle h, float cell_size);
+/* Launch shape of the particle kernels (autotuner): threads per CTA (a
+ * multiple of 32, at most 256) and CTAs per SM of the grid-stride grids, for
+ * the streaming kernels and for the pair kernel.  The result of a step does
+ * not depend on it. */
+BD_API bd_status bd_set_launch_shape(bd_handle h, int block_stream, int ctas_per_sm_stream, int block_pairs,
+                                     int ctas_per_sm_pairs);
 
 /* ------------------------------------------------------------- ensemble */
 

@@ -162,13 +162,17 @@ void build_model(const or_system* s, Model* m) {
     if (s->order[r] == 2 && m->r2[r] > 0.0f) m->max_r = std::max(m->max_r, s->bind_radius[r]);
 }
 
-inline uint32_t pack(uint32_t inst, int sp) { return (inst << 16) | ((uint32_t)sp & 0xFFFFu); }
+inline uint32_t pack(uint32_t inst, int sp) { return (inst << 16) | ((uint32_t)sp & 0x7FFFu); }
+
+// born in this step (uni second product, zeroth order): sorted with the
+// mark, excluded from this step's pair search, cleared in the output
+const uint32_t NEWBORN = 0x8000u;
 
 // Step 1 for slot i: returns the number of records written to out.
 int advance(const Model& m, uint32_t t, uint32_t i, const Rec& in, Rec out[2], uint64_t* ev) {
   const or_system* s = m.s;
   if (in.w == DEAD) return 0;
-  const int sp = (int)(in.w & 0xFFFFu);
+  const int sp = (int)(in.w & 0x7FFFu);
   uint32_t o[4];
   m.rng.block(i, t, T_DIFF, 0, o);
   float g[3];
@@ -205,7 +209,7 @@ int advance(const Model& m, uint32_t t, uint32_t i, const Rec& in, Rec out[2], u
             p[a] = wall(std::fmaf(s->off0[r], d[a], p[a]), s->lo[a], s->hi[a]);
           }
         }
-        out[1] = Rec{b[0], b[1], b[2], pack(s->inst, s->prod1[r])};
+        out[1] = Rec{b[0], b[1], b[2], pack(s->inst, s->prod1[r]) | NEWBORN};
         n = 2;
       }
       break;
@@ -297,8 +301,9 @@ extern "C" int or_step(const or_system* s, uint32_t t, const uint32_t* in, uint3
       float p[3];
       for (int a = 0; a < 3; a++)
         p[a] = std::min(std::fmaf(unit24(o[a]), s->hi[a] - s->lo[a], s->lo[a]), s->hi[a]);
-      born.push_back(Rec{p[0], p[1], p[2], pack(s->inst, s->prod0[r])});
-      if (s->prod1[r] >= 0) born.push_back(Rec{p[0], p[1], p[2], pack(s->inst, s->prod1[r])});
+      const uint32_t mark = s->sorted ? NEWBORN : 0u;
+      born.push_back(Rec{p[0], p[1], p[2], pack(s->inst, s->prod0[r]) | mark});
+      if (s->prod1[r] >= 0) born.push_back(Rec{p[0], p[1], p[2], pack(s->inst, s->prod1[r]) | mark});
     }
   }
 
@@ -345,7 +350,8 @@ extern "C" int or_step(const or_system* s, uint32_t t, const uint32_t* in, uint3
         for (int64_t ii = 0; ii < (int64_t)res.size(); ii++) {
           const uint32_t i = (uint32_t)ii;
           const Rec& a = res[i];
-          const int sa = (int)(a.w & 0xFFFFu);
+          if (a.w & NEWBORN) continue;
+          const int sa = (int)(a.w & 0x7FFFu);
           const int cx = cell_axis(a.x, s->lo[0], s->inv[0], s->dims[0]);
           const int cy = cell_axis(a.y, s->lo[1], s->inv[1], s->dims[1]);
           const int cz = cell_axis(a.z, s->lo[2], s->inv[2], s->dims[2]);
@@ -359,7 +365,8 @@ extern "C" int or_step(const or_system* s, uint32_t t, const uint32_t* in, uint3
                 for (uint32_t j = start[c]; j < start[c + 1]; j++) {
                   if (j <= i) continue;
                   const Rec& b = res[j];
-                  const int r = m.table[(size_t)sa * s->S + (b.w & 0xFFFFu)];
+                  if (b.w & NEWBORN) continue;
+                  const int r = m.table[(size_t)sa * s->S + (b.w & 0x7FFFu)];
                   if (r < 0) continue;
                   const float ex = a.x - b.x, ey = a.y - b.y, ez = a.z - b.z;
                   const float d2 = (ex * ex + ey * ey) + ez * ez;
@@ -393,7 +400,7 @@ extern "C" int or_step(const or_system* s, uint32_t t, const uint32_t* in, uint3
       const Cand& q = cand[k];
       const int r = q.r;
       const Rec ri = res[q.i], rj = res[q.j];
-      const bool i_first = (int)(ri.w & 0xFFFFu) == s->react0[r];
+      const bool i_first = (int)(ri.w & 0x7FFFu) == s->react0[r];
       const uint32_t m1 = i_first ? q.i : q.j, m2 = i_first ? q.j : q.i;
       const Rec& p1 = i_first ? ri : rj;
       const Rec& p2 = i_first ? rj : ri;
@@ -418,6 +425,8 @@ extern "C" int or_step(const or_system* s, uint32_t t, const uint32_t* in, uint3
       res[m2] = n2;
       ev_total[r]++;
     }
+    for (Rec& q : res)
+      if (q.w != DEAD) q.w &= ~NEWBORN;
     npairs = (uint32_t)cand.size();
     if (pairs)
       for (size_t k = 0; k < cand.size() && k < pairs_cap; k++) {

@@ -133,7 +133,7 @@ class OracleSystem:
         out = np.zeros((cap, 4), np.uint32)
         n_out = C.c_uint32()
         cells = np.zeros(self.n_cells + 1, np.uint32) if want_cells else None
-        pcap = 1 << 20
+        pcap = 1 << 22
         pairs = np.zeros((pcap, 4), np.uint32) if want_pairs else None
         n_pairs = C.c_uint32()
         ev = events if events is not None else np.zeros(max(self.R, 1), np.uint64)

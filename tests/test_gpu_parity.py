@@ -97,7 +97,7 @@ def test_contested_pairs_bit_exact():
 def test_reaction_probability_coin_bit_exact():
     s = System((0, 0, 0), (1.5, 1.5, 1.5), dt=1e-3, seed=13, normals="table")
     A, B, Cc, Dd = s.add_species(1.0), s.add_species(0.3), s.add_species(0.5), s.add_species(2.0)
-    r = s.add_reaction(2, [A, B], [Cc, Dd], 30.0)
+    r = s.add_reaction(2, [A, B], [Cc, Dd], 1.5)  # a ~ 0.09 um
     s.set_reaction_probability(r, 0.35)
     s.set_product_placement(r, L.BD_PP_UNBINDRAD, 0.02)
     s.finalize()
@@ -137,11 +137,11 @@ def test_mixed_network_bit_exact():
     s.add_reaction(1, [0], [], 3.0)
     b = s.add_reaction(1, [0], [1, 2], 7.5)
     s.set_product_placement(b, L.BD_PP_UNBINDRAD, 0.05)
-    s.add_reaction(2, [2, 2], [3], 40.0)
+    s.add_reaction(2, [2, 2], [3], 2.0)
     s.add_reaction(1, [3], [], 2.0)
-    p = s.add_reaction(2, [1, 3], [0, 4], 25.0)
+    p = s.add_reaction(2, [1, 3], [0, 4], 0.5)
     s.set_product_placement(p, L.BD_PP_UNBINDRAD, 0.03)
-    s.add_reaction(2, [4, 0], [], 10.0)
+    s.add_reaction(2, [4, 0], [], 1.0)
     s.finalize()
     g = rng(15)
     pos = uniform_positions(g, 5000, (0, 0, 0), (3.0, 2.0, 2.5))
@@ -182,8 +182,8 @@ def test_capacity_growth_replays_exactly():
         s = System((0, 0, 0), (2, 2, 2), dt=1e-3, seed=18, normals="table", capacity=cap)
         s.add_species(1.0)
         s.add_species(1.0)
-        s.add_reaction(1, [0], [0, 1], 50.0)
-        s.add_reaction(2, [0, 1], [1], 5.0)
+        s.add_reaction(1, [0], [0, 1], 50.0)   # ~5% of the A give birth every step
+        s.add_reaction(2, [0, 1], [0], 0.2)
         s.finalize()
         g = rng(18)
         s.set_particles(uniform_positions(g, 4000, (0, 0, 0), (2, 2, 2)), np.zeros(4000, np.int32))
