@@ -72,7 +72,8 @@ __device__ __forceinline__ void normals3(const U4& r, const float* __restrict__ 
     // errors ~1e-6, far below the statistical resolution of the step
     const float a = u24_to_unit(r.x) + 2.98023223876953125e-08f;  // (0, 1)
     const float c = u24_to_unit(r.z) + 2.98023223876953125e-08f;
-    const float la = -2.0f * __logf(a), lc = -2.0f * __logf(c);  // > 0
+    // __logf may round to 0 just below 1: keep the radius finite (0)
+    const float la = fmaxf(-2.0f * __logf(a), 1e-30f), lc = fmaxf(-2.0f * __logf(c), 1e-30f);
     const float ra = la * rsqrtf(la);
     const float rc = lc * rsqrtf(lc);
     float sa, ca, sc, cc;

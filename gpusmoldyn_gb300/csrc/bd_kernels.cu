@@ -403,6 +403,27 @@ __device__ __forceinline__ float dist2(const float4& a, const float4& b) {
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// Append candidate pair (lo < hi, canonical slots) of local reaction b,
+// after its coin when the reaction probability is below 1.
+__device__ __forceinline__ void emit_pair(const KParams& p, DevCtrl* c, uint32_t lo, uint32_t hi, int32_t b,
+                                          float prob, uint32_t inst, const DevInstance* __restrict__ Ip,
+                                          uint32_t cbase) {
+  if (prob < 1.0f) {
+    const uint32_t base_new = __ldg(&p.cell_start[cbase]);
+    const U4 u = philox(U4{lo - base_new, __ldg(&p.inst_step[inst]), kTagBimCoin, hi - base_new},
+                        __ldg(&Ip->key_lo), __ldg(&Ip->key_hi));
+    if (!(u32_to_unit(u.x) < prob)) return;
+  }
+  const uint32_t idx = atomicAdd(&c->n_pairs, 1u);
+  if (idx < p.pair_cap) p.pairs[idx] = DevPair{lo, hi, (uint32_t)b | (inst << 16), 0u};
+  else atomicOr(&c->status, kStatPairs);
+}
+
+constexpr uint32_t kRankCache = 16;
+
+// One thread per cell: write the cell's records in canonical order, then
+// test each pair of the cell once and, for members within the largest
+// binding radius of a face, the members of the neighbouring cells.
 template <bool kHasBim>
 __global__ void __launch_bounds__(256) k_pairs(KParams p) {
   DevCtrl* c = p.ctrl;
@@ -410,87 +431,86 @@ __global__ void __launch_bounds__(256) k_pairs(KParams p) {
   const uint32_t cur = ld_u32(&c->cur);
   float4* __restrict__ nx = next_state(p, cur);
   const float4* __restrict__ sc = p.scatter;
-  const uint32_t n = ld_u32(&c->n_sorted);
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const float4 r = sc[i];
-    const uint32_t w = rec_w(r);
-    const uint32_t inst = w >> 16, sp = w & kSpeciesMask;
+  for (uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x; cell < p.n_cells; cell += stride) {
+    const uint32_t s0 = __ldg(&p.cell_start[cell]), e0 = __ldg(&p.cell_start[cell + 1]);
+    if (e0 <= s0) continue;
+    const uint32_t n = e0 - s0;
+    uint32_t rk[kRankCache];
+    for (uint32_t a = 0; a < n; ++a) {
+      const float4 ra = sc[s0 + a];
+      const uint32_t rank = canonical_rank(sc, s0, e0, s0 + a, ra);
+      if (a < kRankCache) rk[a] = rank;
+      // the newborn mark lives only within this step
+      nx[s0 + rank] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
+    }
+    if (!kHasBim) continue;
+    const uint32_t inst = rec_w(sc[s0]) >> 16;  // a cell belongs to one instance
+    if (!advancing(__ldg(&p.inst_flags[inst]))) continue;
     const DevInstance* __restrict__ Ip = p.inst + inst;
-    // the instance's grid in registers (no reloads across the stores below)
     const float lo0 = __ldg(&Ip->lo[0]), lo1 = __ldg(&Ip->lo[1]), lo2 = __ldg(&Ip->lo[2]);
     const float iv0 = __ldg(&Ip->inv[0]), iv1 = __ldg(&Ip->inv[1]), iv2 = __ldg(&Ip->inv[2]);
-    const uint32_t d0 = __ldg(&Ip->dims[0]), d1 = __ldg(&Ip->dims[1]), d2 = __ldg(&Ip->dims[2]);
-    const uint32_t cbase = __ldg(&Ip->cell_base);
-    const int cx = cell_coord(r.x, lo0, iv0, d0);
-    const int cy = cell_coord(r.y, lo1, iv1, d1);
-    const int cz = cell_coord(r.z, lo2, iv2, d2);
-    const uint32_t key = cbase + ((uint32_t)cz * d1 + (uint32_t)cy) * d0 + (uint32_t)cx;
-    const uint32_t s0 = __ldg(&p.cell_start[key]), e0 = __ldg(&p.cell_start[key + 1]);
-    if (i < s0 || i >= e0) {
-      atomicOr(&c->status, kStatBounds);
-      continue;
-    }
-    const uint32_t ci = s0 + canonical_rank(sc, s0, e0, i, r);
-    // the newborn mark lives only within this step
-    nx[ci] = make_float4(r.x, r.y, r.z, __uint_as_float(w & ~kNewborn));
-    if (!kHasBim || (w & kNewborn)) continue;
-    if (!advancing(__ldg(&p.inst_flags[inst]))) continue;
-    const uint32_t block = __ldg(&Ip->block);
-    const float max_r = __ldg(&p.species[block * p.S + sp].max_r);
-    if (max_r <= 0.0f) continue;
     const float cl0 = __ldg(&Ip->cell[0]), cl1 = __ldg(&Ip->cell[1]), cl2 = __ldg(&Ip->cell[2]);
-
-    // distances to the six faces of the cell, for pruning neighbour cells
-    const float fx = __fsub_rn(__fmul_rn(__fsub_rn(r.x, lo0), iv0), (float)cx);
-    const float fy = __fsub_rn(__fmul_rn(__fsub_rn(r.y, lo1), iv1), (float)cy);
-    const float fz = __fsub_rn(__fmul_rn(__fsub_rn(r.z, lo2), iv2), (float)cz);
-    const float lox = fx * cl0, hix = (1.0f - fx) * cl0;
-    const float loy = fy * cl1, hiy = (1.0f - fy) * cl1;
-    const float loz = fz * cl2, hiz = (1.0f - fz) * cl2;
-    const float need = max_r + p.prune_margin * fminf(cl0, fminf(cl1, cl2));
-    const float need2 = need * need;
-    const int32_t* __restrict__ row = p.bim_table + sp * p.S;
-
-    // only the neighbours across faces closer than the largest binding
-    // radius can hold a partner: usually the particle's own cell alone
-    const int zlo = (cz > 0 && loz <= need) ? -1 : 0, zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
-    const int ylo = (cy > 0 && loy <= need) ? -1 : 0, yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
-    const int xlo = (cx > 0 && lox <= need) ? -1 : 0, xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-      const int nz_ = cz + dz;
-      const float ddz = dz < 0 ? loz : (dz > 0 ? hiz : 0.0f);
-      for (int dy = ylo; dy <= yhi; ++dy) {
-        const int ny_ = cy + dy;
-        const float ddy = dy < 0 ? loy : (dy > 0 ? hiy : 0.0f);
-        for (int dx = xlo; dx <= xhi; ++dx) {
-          const int nx_ = cx + dx;
-          const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
-          if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
-          const uint32_t nkey = cbase + ((uint32_t)nz_ * d1 + (uint32_t)ny_) * d0 + (uint32_t)nx_;
-          const uint32_t ns = __ldg(&p.cell_start[nkey]), ne = __ldg(&p.cell_start[nkey + 1]);
-          for (uint32_t m = ns; m < ne; ++m) {
-            if (m == i) continue;
-            const float4 q = sc[m];
-            const uint32_t wq = rec_w(q);
-            if (wq & kNewborn) continue;
-            const int32_t b = __ldg(&row[wq & kSpeciesMask]);
-            if (b < 0) continue;
-            const DevBim& br = p.bim[block * p.B + (uint32_t)b];
-            if (dist2(r, q) > __ldg(&br.r2)) continue;
-            const uint32_t cj = ns + canonical_rank(sc, ns, ne, m, q);
-            if (ci >= cj) continue;  // the pair is reported by its lower slot
-            if (__ldg(&br.prob) < 1.0f) {
-              const uint32_t base_new = __ldg(&p.cell_start[cbase]);
-              const U4 u = philox(U4{ci - base_new, __ldg(&p.inst_step[inst]), kTagBimCoin, cj - base_new},
-                                  __ldg(&Ip->key_lo), __ldg(&Ip->key_hi));
-              if (!(u32_to_unit(u.x) < br.prob)) continue;
-            }
-            const uint32_t idx = atomicAdd(&c->n_pairs, 1u);
-            if (idx < p.pair_cap) {
-              p.pairs[idx] = DevPair{ci, cj, (uint32_t)b | (inst << 16), 0u};
-            } else {
-              atomicOr(&c->status, kStatPairs);
+    const uint32_t d0 = __ldg(&Ip->dims[0]), d1 = __ldg(&Ip->dims[1]), d2 = __ldg(&Ip->dims[2]);
+    const uint32_t cbase = __ldg(&Ip->cell_base), block = __ldg(&Ip->block);
+    const uint32_t local = cell - cbase;
+    const int cx = (int)(local % d0), cy = (int)((local / d0) % d1), cz = (int)(local / (d0 * d1));
+    const float margin = p.prune_margin * fminf(cl0, fminf(cl1, cl2));
+    for (uint32_t a = 0; a < n; ++a) {
+      const float4 ra = sc[s0 + a];
+      const uint32_t wa = rec_w(ra);
+      if (wa & kNewborn) continue;
+      const uint32_t sa = wa & kSpeciesMask;
+      const float max_r = __ldg(&p.species[block * p.S + sa].max_r);
+      if (max_r <= 0.0f) continue;
+      const uint32_t ca = s0 + (a < kRankCache ? rk[a] : canonical_rank(sc, s0, e0, s0 + a, ra));
+      const int32_t* __restrict__ row = p.bim_table + sa * p.S;
+      // pairs inside the cell, each once
+      for (uint32_t bb = a + 1; bb < n; ++bb) {
+        const float4 rb = sc[s0 + bb];
+        const uint32_t wb = rec_w(rb);
+        if (wb & kNewborn) continue;
+        const int32_t b = __ldg(&row[wb & kSpeciesMask]);
+        if (b < 0) continue;
+        const DevBim& br = p.bim[block * p.B + (uint32_t)b];
+        if (dist2(ra, rb) > __ldg(&br.r2)) continue;
+        const uint32_t cb = s0 + (bb < kRankCache ? rk[bb] : canonical_rank(sc, s0, e0, s0 + bb, rb));
+        emit_pair(p, c, min(ca, cb), max(ca, cb), b, __ldg(&br.prob), inst, Ip, cbase);
+      }
+      // neighbour cells across faces closer than the largest binding radius;
+      // the pair is reported from the side with the lower canonical slot
+      const float fx = __fsub_rn(__fmul_rn(__fsub_rn(ra.x, lo0), iv0), (float)cx);
+      const float fy = __fsub_rn(__fmul_rn(__fsub_rn(ra.y, lo1), iv1), (float)cy);
+      const float fz = __fsub_rn(__fmul_rn(__fsub_rn(ra.z, lo2), iv2), (float)cz);
+      const float lox = fx * cl0, hix = (1.0f - fx) * cl0;
+      const float loy = fy * cl1, hiy = (1.0f - fy) * cl1;
+      const float loz = fz * cl2, hiz = (1.0f - fz) * cl2;
+      const float need = max_r + margin, need2 = need * need;
+      const int zlo = (cz > 0 && loz <= need) ? -1 : 0, zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
+      const int ylo = (cy > 0 && loy <= need) ? -1 : 0, yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
+      const int xlo = (cx > 0 && lox <= need) ? -1 : 0, xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
+      if ((zlo | zhi | ylo | yhi | xlo | xhi) == 0) continue;
+      for (int dz = zlo; dz <= zhi; ++dz) {
+        const float ddz = dz < 0 ? loz : (dz > 0 ? hiz : 0.0f);
+        for (int dy = ylo; dy <= yhi; ++dy) {
+          const float ddy = dy < 0 ? loy : (dy > 0 ? hiy : 0.0f);
+          for (int dx = xlo; dx <= xhi; ++dx) {
+            if (dx == 0 && dy == 0 && dz == 0) continue;
+            const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
+            if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
+            const uint32_t nkey =
+                cbase + ((uint32_t)(cz + dz) * d1 + (uint32_t)(cy + dy)) * d0 + (uint32_t)(cx + dx);
+            const uint32_t ns = __ldg(&p.cell_start[nkey]), ne = __ldg(&p.cell_start[nkey + 1]);
+            for (uint32_t m = ns; m < ne; ++m) {
+              const float4 q = sc[m];
+              const uint32_t wq = rec_w(q);
+              if (wq & kNewborn) continue;
+              const int32_t b = __ldg(&row[wq & kSpeciesMask]);
+              if (b < 0) continue;
+              const DevBim& br = p.bim[block * p.B + (uint32_t)b];
+              if (dist2(ra, q) > __ldg(&br.r2)) continue;
+              const uint32_t cq = ns + canonical_rank(sc, ns, ne, m, q);
+              if (ca < cq) emit_pair(p, c, ca, cq, b, __ldg(&br.prob), inst, Ip, cbase);
             }
           }
         }

@@ -81,14 +81,16 @@ def test_reflection_keeps_uniform_density():
 
 
 def test_bimolecular_rate_matches_rxnparam():
-    """A + B -> B (B catalytic): -d ln N_A / dt = k_eff rho_B with
+    """B + A -> B with immobile B catalysts (D_B = 0, so the product stays
+    exactly where B was and the B's stay uniform) and D_A = 2, the c2
+    mutual diffusion: -d ln N_A / dt = k_eff rho_B with
     k_eff = numrxnrate(step, a, -1)/dt x (1 + 2R/sqrt(pi D T)), the time
     average of the Smoluchowski transient over the run (R = k / 4 pi D)."""
     side, rho, dt, k, steps = 50.0, 10.0, 5e-4, 0.05, 2000
     n = int(rho * side ** 3)
     s = System((0, 0, 0), (side,) * 3, dt=dt, seed=24)
-    A, B = s.add_species(1.0), s.add_species(1.0)
-    r = s.add_reaction(2, [A, B], [B], k)
+    A, B = s.add_species(2.0), s.add_species(0.0)
+    r = s.add_reaction(2, [B, A], [B], k)
     s.finalize()
     a = s.reaction_info(r)["bind_radius"]
     g = rng(24)
