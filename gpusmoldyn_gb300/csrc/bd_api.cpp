@@ -1360,6 +1360,7 @@ BD_API bd_status bd_set_launch_shape(bd_handle h, int bs, int cs, int bp, int cp
   if (cs < 1 || cs > 64 || cp < 1 || cp > 64) return BD_ERR_INVALID_ARGUMENT;
   h->shape.block_stream = bs;
   h->shape.grid_stream = h->n_sm * cs;
+  h->shape.hi_occupancy = bs == 256 && cs == 6;
   h->shape.block_pairs = bp;
   h->shape.grid_pairs = h->n_sm * cp;
   if (h->host_only || !h->have_particles) return BD_OK;

@@ -282,8 +282,10 @@ __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
   }
 }
 
-template <bool kTable>
-__global__ void __launch_bounds__(256) k_count(KParams p) {
+// kMinBlocks = 6 caps registers at 40 for 75% occupancy (a few spills);
+// the launch shape picks the variant.
+template <bool kTable, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
   const DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
   const uint32_t cur = ld_u32(&c->cur);
@@ -357,8 +359,8 @@ __global__ void __launch_bounds__(1024) k_scan_down(KParams p) {
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) p.cell_start[p.n_cells] = ld_u32(&c->n_sorted);
 }
 
-template <bool kTable>
-__global__ void __launch_bounds__(256) k_scatter(KParams p) {
+template <bool kTable, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
   DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
   const uint32_t cur = ld_u32(&c->cur);
@@ -760,8 +762,14 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     done("k_finalize_inplace");
     return n;
   }
-  if (table) k_count<true><<<gs, bs, 0, s>>>(p);
-  else k_count<false><<<gs, bs, 0, s>>>(p);
+  const bool hi_occ = shape.hi_occupancy;
+  if (table) {
+    if (hi_occ) k_count<true, 6><<<gs, bs, 0, s>>>(p);
+    else k_count<true, 1><<<gs, bs, 0, s>>>(p);
+  } else {
+    if (hi_occ) k_count<false, 6><<<gs, bs, 0, s>>>(p);
+    else k_count<false, 1><<<gs, bs, 0, s>>>(p);
+  }
   done("k_count");
   k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
   done("k_scan_tiles");
@@ -769,8 +777,13 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   done("k_scan_top");
   k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
   done("k_scan_down");
-  if (table) k_scatter<true><<<gs, bs, 0, s>>>(p);
-  else k_scatter<false><<<gs, bs, 0, s>>>(p);
+  if (table) {
+    if (hi_occ) k_scatter<true, 6><<<gs, bs, 0, s>>>(p);
+    else k_scatter<true, 1><<<gs, bs, 0, s>>>(p);
+  } else {
+    if (hi_occ) k_scatter<false, 6><<<gs, bs, 0, s>>>(p);
+    else k_scatter<false, 1><<<gs, bs, 0, s>>>(p);
+  }
   done("k_scatter");
   if (has_bim) k_pairs<true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
   else k_pairs<false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);

@@ -44,6 +44,7 @@ struct LaunchShape {
   int grid_stream;            // blocks of the grid-stride particle kernels
   int block_stream;           // threads per block of those kernels
   int grid_pairs, block_pairs;
+  bool hi_occupancy;          // 40-register variants of k_count / k_scatter (6 CTAs/SM)
 };
 
 // Called after each kernel of a step is enqueued (stage name); lets the
