@@ -55,11 +55,13 @@ __device__ __forceinline__ double u53_to_unit(uint32_t a, uint32_t b) {
   return (double)m * 1.1102230246251565e-16;
 }
 
-// Three standard normals from one Philox block.
-// Table mode: the top 12 bits of each word index the 4096 quantiles of
+// Three standard normals from words x, y, z of one Philox block; word w is
+// left for the first first-order coin.
+// Table mode: the top 12 bits of x, y, z index the 4096 quantiles of
 // N(0,1) (the reference's gaussianLookupTable, particles_kernel.cu:156-162).
 // Box-Muller mode (G. E. P. Box and M. E. Muller, Ann. Math. Stat. 29:610,
-// 1958): two pairs of 24-bit uniforms give four normals, three are used.
+// 1958): two pairs of 24-bit uniforms give four normals, three are used;
+// the fourth uniform is made of the low bytes of x, y, z.
 template <bool kTable>
 __device__ __forceinline__ void normals3(const U4& r, const float* __restrict__ table, float& g0,
                                          float& g1, float& g2) {
@@ -78,7 +80,8 @@ __device__ __forceinline__ void normals3(const U4& r, const float* __restrict__ 
     const float rc = lc * rsqrtf(lc);
     float sa, ca, sc, cc;
     __sincosf(6.2831853071795865f * u24_to_unit(r.y), &sa, &ca);
-    __sincosf(6.2831853071795865f * u24_to_unit(r.w), &sc, &cc);
+    const uint32_t low = ((r.x & 0xFFu) << 24) | ((r.y & 0xFFu) << 16) | ((r.z & 0xFFu) << 8);
+    __sincosf(6.2831853071795865f * u24_to_unit(low), &sc, &cc);
     g0 = ra * ca;
     g1 = ra * sa;
     g2 = rc * cc;

@@ -127,11 +127,12 @@ __device__ __forceinline__ void advance_real(const KParams& p, const float4* __r
   uint32_t species = sp;
   int n = 1;
 
-  U4 coins{0u, 0u, 0u, 0u};
+  // coin 0 is the diffusion block's spare word; coins 1.. come 4 per block
+  U4 coins = rn;
   for (uint32_t k = 0; k < S.uni_count; ++k) {
-    if ((k & 3u) == 0) coins = philox(U4{local, t, kTagUniCoin | (k >> 2), 0u}, k0, k1);
+    if (k > 0 && ((k - 1) & 3u) == 0) coins = philox(U4{local, t, kTagUniCoin | ((k - 1) >> 2), 0u}, k0, k1);
     const DevUni& u = p.uni[I.block * p.U + S.uni_begin + k];
-    if (u32_to_unit(word_of(coins, k)) < u.prob) {
+    if (u32_to_unit(k == 0 ? rn.w : word_of(coins, k - 1)) < u.prob) {
       if (kCount) atomicAdd(&p.pending[(size_t)inst * p.R + u.rxn], 1ull);
       if (u.prod0 < 0) return;  // decay: no record
       species = (uint32_t)u.prod0;

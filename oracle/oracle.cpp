@@ -181,7 +181,8 @@ int advance(const Model& m, uint32_t t, uint32_t i, const Rec& in, Rec out[2], u
   } else {
     const float ua = unit24(o[0]) + 2.98023223876953125e-08f, uc = unit24(o[2]) + 2.98023223876953125e-08f;
     const float ra = sqrtf(-2.0f * logf(ua)), rc = sqrtf(-2.0f * logf(uc));
-    const float pa = 6.283185307179586f * unit24(o[1]), pc = 6.283185307179586f * unit24(o[3]);
+    const uint32_t low = ((o[0] & 0xFFu) << 24) | ((o[1] & 0xFFu) << 16) | ((o[2] & 0xFFu) << 8);
+    const float pa = 6.283185307179586f * unit24(o[1]), pc = 6.283185307179586f * unit24(low);
     g[0] = ra * cosf(pa);
     g[1] = ra * sinf(pa);
     g[2] = rc * cosf(pc);
@@ -191,11 +192,14 @@ int advance(const Model& m, uint32_t t, uint32_t i, const Rec& in, Rec out[2], u
   int species = sp;
   int n = 1;
   const std::vector<int>& list = m.uni[sp];
+  // the first coin is the diffusion block's fourth word, the others come
+  // four per block of the first-order stream
   uint32_t coin[4] = {0, 0, 0, 0};
   for (size_t k = 0; k < list.size(); k++) {
-    if (k % 4 == 0) m.rng.block(i, t, T_UNI | (uint32_t)(k / 4), 0, coin);
+    if (k > 0 && (k - 1) % 4 == 0) m.rng.block(i, t, T_UNI | (uint32_t)((k - 1) / 4), 0, coin);
     const int r = list[k];
-    if (unit32(coin[k % 4]) < s->prob[r]) {
+    const uint32_t word = k == 0 ? o[3] : coin[(k - 1) % 4];
+    if (unit32(word) < s->prob[r]) {
       if (ev) ev[r]++;
       if (s->prod0[r] < 0) return 0;
       species = s->prod0[r];
