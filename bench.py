@@ -175,14 +175,16 @@ def traffic_from_profiles(kernel, workload):
     return None
 
 
-def algorithmic_bytes(kernel, n_in, n_out, n_cells):
+def algorithmic_bytes(kernel, n_in, n_out, n_cells, binned=True):
     """Bytes a kernel must move at minimum (16-byte records, 4-byte cell words)."""
     table = {
+        "k_bin": 16 * n_in + 16 * n_out + 4 * n_cells,      # read records, write bins, histogram
         "k_count": 16 * n_in + 4 * n_cells,                 # read records, write histogram
         "k_scan_tiles": 4 * n_cells,
         "k_scan_down": 8 * n_cells,                          # read counts, write starts
         "k_scatter": 16 * n_in + 16 * n_out + 8 * n_cells,   # read + write records, starts + counts
-        "k_pairs": 32 * n_out + 4 * n_cells,                 # read + write records, starts
+        # read + write records, starts (+ clear the bin counts)
+        "k_pairs_cells": 32 * n_out + (8 if binned else 4) * n_cells,
         "k_diffuse": 32 * n_in,
     }
     return table.get(kernel)
@@ -239,9 +241,7 @@ def cpu_oracle_rate(n, steps, threads, budget_s=None, warmup=1):
     o = orc.OracleSystem(s, threads=threads)
     from gpusmoldyn_gb300 import configs
 
-    g = configs.rng(3)
-    pos = configs.uniform_positions(g, n, (0, 0, 0), (side, side, side))
-    sp = (np.arange(n) % 8).astype(np.int32)
+    pos, sp = configs.c3_particles(n, side)
     recs = orc.records(pos, sp)
     for t in range(max(warmup, 1)):
         recs = o.step(t, recs)["recs"]
@@ -319,7 +319,8 @@ def run_gb300(args, dist):
     prof = s.profile_steps(prof_steps)
     dom = max(prof, key=prof.get)
     n_now = s.count()
-    alg = algorithmic_bytes(dom, n_now, n_now, n_cells)
+    binned = "k_bin" in prof
+    alg = algorithmic_bytes(dom, n_now, n_now, n_cells, binned)
     peak, peak_kind = measured_peak()
     roof = None
     if alg:
@@ -328,7 +329,7 @@ def run_gb300(args, dist):
                 "frac": achieved / peak, "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": alg,
                 "traffic": traffic_from_profiles(dom, args.workload)}
-    step_alg = sum(v for v in (algorithmic_bytes(k, n_now, n_now, n_cells) for k in prof) if v)
+    step_alg = sum(v for v in (algorithmic_bytes(k, n_now, n_now, n_cells, binned) for k in prof) if v)
     step_roof = {"bytes_per_step": step_alg, "achieved_gbs": step_alg / (ms / args.steps / 1e3) / 1e9,
                  "frac": step_alg / (ms / args.steps / 1e3) / 1e9 / peak}
     s.close()
@@ -339,6 +340,7 @@ def run_gb300(args, dist):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox uniform positions)",
         "config": {"workload": desc, "particles": int(n0) * dist.world,
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
+                   "particles_end": int(n1) * dist.world, "sort": "binned" if binned else "compact",
                    "normals": "box-muller (Philox)", "cells": n_cells, "l2": "state 256 MB > 129 MB L2, no flush"},
         "clocks": clk, "gpu_launches": kps * args.steps,
         "kernel_ms_per_step": {k: v / prof_steps for k, v in prof.items()},

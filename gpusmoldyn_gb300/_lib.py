@@ -31,6 +31,10 @@ BD_ERR_DEVICE_STATE = 24
 BD_NORMALS_BOXMULLER = 0
 BD_NORMALS_TABLE = 1
 
+BD_SORT_AUTO = 0
+BD_SORT_COMPACT = 1
+BD_SORT_BINNED = 2
+
 BD_PP_DEFAULT = 0
 BD_PP_PGEM = 1
 BD_PP_PGEMMAX = 2
@@ -44,7 +48,7 @@ class bd_config(C.Structure):
     _fields_ = [("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("dt", C.c_float),
                 ("seed", C.c_uint64), ("capacity", C.c_uint64), ("cell_size", C.c_float),
                 ("cell_occupancy", C.c_float), ("normal_mode", C.c_int), ("device", C.c_int),
-                ("pair_capacity", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+                ("pair_capacity", C.c_uint32), ("sort_mode", C.c_uint32), ("reserved", C.c_uint32 * 6)]
 
 
 class bd_reaction_info(C.Structure):

@@ -9,7 +9,8 @@ box from numpy's Philox generator with the configuration's seed.
   k_off 10, dt 0.5 ms.
 * c3: 8-species network, 16M particles in a 200 um cube, 12 reactions
   (2 zeroth, 4 first, 5 hetero- and 1 homodimeric second order), D log-uniform
-  0.1-10, rates log-uniform over a decade, dt 1 ms, production balancing loss.
+  0.1-10, rates log-uniform over a decade, dt 1 ms, started at the network's
+  stationary composition so the particle count stays put.
 * c4: 256 instances of the c2 network, N log-uniform 1e3-1e6 (about 37M),
   per-instance D and k_on scaled log-uniform over a decade, c2 density.
 * c5: serving jobs, c3 network, N log-uniform 1e3-5e6, steps U[100, 10000],
@@ -79,66 +80,127 @@ def build_c2(n_a=500000, n_b=500000, side=60.0, seed=2, normals="boxmuller", **k
 
 # ---------------------------------------------------------------------- c3
 def c3_network(seed=3):
-    """Species diffusion coefficients and the 12 reactions (order, reactants,
-    products, rate) of the 8-species network; zeroth-order rates are per
-    volume and set so production balances loss at the initial composition."""
+    """Species diffusion coefficients and the 10 non-zeroth reactions (order,
+    reactants, products, rate) of the 8-species network.
+
+    S0 and S1 are made by the two zeroth-order reactions; S4/S5 and S6/S7
+    are carrier pairs whose totals are conserved; S3 -> 0 is the only exit.
+    Every species is made and consumed, so the network has one stable
+    stationary composition (c3_steady_state) and a run started there keeps
+    its particle count.  Rates are log-uniform over one decade: first order
+    0.01-0.1 /s, second order 0.01-0.1 um^3/s."""
     g = rng(seed)
     D = np.exp(g.uniform(math.log(0.1), math.log(10.0), 8)).astype(np.float32)
-    k1 = np.exp(g.uniform(math.log(1.0), math.log(10.0), 4))
+    k1 = np.exp(g.uniform(math.log(0.01), math.log(0.1), 4))
     k2 = np.exp(g.uniform(math.log(0.01), math.log(0.1), 6))
     rx = [
-        (1, [2], [], k1[0]),          # S2 -> 0
-        (1, [3], [], k1[1]),          # S3 -> 0
-        (1, [4], [2], k1[2]),         # S4 -> S2
-        (1, [5], [3], k1[3]),         # S5 -> S3
         (2, [0, 1], [2], k2[0]),      # S0 + S1 -> S2
-        (2, [0, 3], [4], k2[1]),      # S0 + S3 -> S4
-        (2, [1, 4], [5], k2[2]),      # S1 + S4 -> S5
-        (2, [2, 6], [7], k2[3]),      # S2 + S6 -> S7
-        (2, [5, 7], [6], k2[4]),      # S5 + S7 -> S6
-        (2, [6, 6], [7], k2[5]),      # S6 + S6 -> S7
+        (1, [2], [3], k1[0]),         # S2 -> S3
+        (2, [3, 4], [5], k2[1]),      # S3 + S4 -> S5
+        (1, [5], [4], k1[1]),         # S5 -> S4
+        (2, [0, 6], [7], k2[2]),      # S0 + S6 -> S7
+        (2, [1, 6], [7], k2[3]),      # S1 + S6 -> S7
+        (1, [7], [6], k1[2]),         # S7 -> S6
+        (2, [2, 4], [5], k2[4]),      # S2 + S4 -> S5
+        (2, [2, 2], [3], k2[5]),      # S2 + S2 -> S3
+        (1, [3], [], k1[3]),          # S3 -> 0
     ]
     return D, rx
 
 
-def c3_zeroth_rate(D, rx, density):
-    """Production per unit volume and time that balances the loss of
-    particles at a uniform composition of `density` per species."""
-    rho = density / 8.0
-    loss = 0.0
+def _mass_action(rho, z, rx):
+    """d rho / dt of the well-mixed network; a homodimeric A + A reaction of
+    rate k fires k rho_A^2 times per unit volume and time (its binding
+    radius is computed for rate 2k)."""
+    d = np.zeros(len(rho))
+    d[0] += z
+    d[1] += z
     for order, rc, pr, k in rx:
-        if order == 1 and not pr:
-            loss += k * rho
-        if order == 2:
-            loss += (len(rc) - len(pr)) * k * rho * rho * (0.5 if rc[0] == rc[1] else 1.0)
-    return loss / 2.0
+        r = k * rho[rc[0]] if order == 1 else k * rho[rc[0]] * rho[rc[1]]
+        for a in rc:
+            d[a] -= r
+        for b in pr:
+            d[b] += r
+    return d
+
+
+def c3_steady_state(rx, density):
+    """Zeroth-order rate z (per unit volume and time, each of S0 and S1) and
+    species fractions of the stationary well-mixed state with total density
+    `density`, each carrier pair holding a quarter of it.  Newton's method
+    on the 6 independent rate equations, the 2 carrier totals and the total."""
+    quarter = density / 4.0
+
+    def F(x):
+        rho, z = x[:8], x[8]
+        d = _mass_action(rho, z, rx)
+        return np.array([d[0], d[1], d[2], d[3], d[4], d[6], rho[4] + rho[5] - quarter,
+                         rho[6] + rho[7] - quarter, rho.sum() - density])
+
+    x = np.full(9, density / 8.0)
+    x[8] = 1e-3 * density
+    for _ in range(100):
+        f = F(x)
+        if np.max(np.abs(f)) < 1e-13 * density:
+            break
+        J = np.empty((9, 9))
+        for j in range(9):
+            e = np.zeros(9)
+            e[j] = 1e-7 * max(abs(x[j]), 1e-6)
+            J[:, j] = (F(x + e) - f) / e[j]
+        dx = np.linalg.solve(J, -f)
+        t = 1.0
+        while np.any(x + t * dx <= 0):
+            t *= 0.5
+        x = x + t * dx
+    else:
+        raise RuntimeError("c3 steady state did not converge")
+    return float(x[8]), x[:8] / density
+
+
+def c3_species(n, frac):
+    """n species ids with the stationary fractions (largest remainders)."""
+    want = np.asarray(frac) * n
+    cnt = np.floor(want).astype(np.int64)
+    rest = n - int(cnt.sum())
+    cnt[np.argsort(-(want - cnt))[:rest]] += 1
+    return np.repeat(np.arange(len(frac), dtype=np.int32), cnt)
+
+
+def c3_add_network(s, density, network_seed=3):
+    """Species and the 12 reactions of the c3 network on a System; returns
+    the stationary species fractions."""
+    D, rx = c3_network(network_seed)
+    for d in D:
+        s.add_species(float(d))
+    z, frac = c3_steady_state(rx, density)
+    s.add_reaction(0, [], [0], z)
+    s.add_reaction(0, [], [1], z)
+    for order, rc, pr, k in rx:
+        s.add_reaction(order, rc, pr, float(k))
+    return frac
 
 
 def c3_system(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
     """The c3 network in a `side` cube, finalized, without particles."""
     s = System((0, 0, 0), (side, side, side), dt=1e-3, seed=seed, normals=normals, **kw)
-    D, rx = c3_network(network_seed)
-    for d in D:
-        s.add_species(float(d))
-    z = c3_zeroth_rate(D, rx, n / side ** 3)
-    s.add_reaction(0, [], [0], z)
-    s.add_reaction(0, [], [1], z)
-    for order, rc, pr, k in rx:
-        s.add_reaction(order, rc, pr, float(k))
+    c3_add_network(s, n / side ** 3, network_seed)
     s.finalize()
     return s
 
 
-def c3_particles(n=16_000_000, side=200.0, seed=3):
+def c3_particles(n=16_000_000, side=200.0, seed=3, network_seed=3):
+    """n particles, uniform in the cube, at the stationary composition."""
     g = rng(seed)
     pos = uniform_positions(g, n, (0, 0, 0), (side, side, side))
-    sp = (np.arange(n) % 8).astype(np.int32)
-    return pos, sp
+    _, rx = c3_network(network_seed)
+    _, frac = c3_steady_state(rx, n / side ** 3)
+    return pos, c3_species(n, frac)
 
 
 def build_c3(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
     s = c3_system(n, side, seed, normals, network_seed, **kw)
-    s.set_particles(*c3_particles(n, side, seed))
+    s.set_particles(*c3_particles(n, side, seed, network_seed))
     return s
 
 

@@ -28,6 +28,8 @@ using namespace bd;
 namespace {
 
 constexpr int kGraphBatch = 16;
+// Largest bin array the automatic sort mode accepts.
+constexpr uint64_t kBinBudgetBytes = 32ull << 30;
 
 thread_local std::string g_last_error;
 
@@ -92,14 +94,17 @@ struct bd_system {
   DevBuf<float> dgauss;
   DevBuf<uint32_t> inst_step, inst_slot_base, zero_off;
   DevBuf<unsigned long long> events, pending;
-  DevBuf<float4> state0, state1, scatter;
-  DevBuf<uint32_t> best, cell_count, cell_start, tile_sums;
+  DevBuf<float4> state0, state1, scatter, bins;
+  DevBuf<uint32_t> best, cell_count, cell_start, tile_sums, big, rank_scratch;
   DevBuf<DevPair> pairs;
 
   std::vector<DevInstance> hinst;
   uint32_t n_cells = 0, n_tiles = 0;
   uint64_t capacity = 0;
   uint32_t pair_cap = 0;
+  bool binned = false;             // Path::kBinned (else the compact counting sort)
+  uint32_t bin_cap = 0;            // records per cell bin
+  std::vector<uint64_t> plan_n;    // particles each instance's grid was planned for
   bool have_particles = false;
   uint64_t target_step = 0;  // absolute step the enqueued work ends at
   float cell_override = 0.0f;
@@ -120,6 +125,7 @@ struct bd_system {
   bool diffuse_only() const {
     return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products && !server;
   }
+  Path path() const { return diffuse_only() ? Path::kDiffuseOnly : (binned ? Path::kBinned : Path::kSorted); }
   int n_inst() const { return (int)idesc.size(); }
 };
 
@@ -136,6 +142,11 @@ KParams make_params(bd_system* h) {
   p.state[0] = h->state0.p;
   p.state[1] = h->state1.p;
   p.scatter = h->scatter.p;
+  p.bins = h->bins.p;
+  p.bin_cap = h->bin_cap;
+  p.big = h->big.p;
+  p.rank_scratch = h->rank_scratch.p;
+  p.big_cap = (uint32_t)h->big.n;
   p.ctrl = h->ctrl.p;
   p.inst = h->dinst.p;
   p.species = h->dspecies.p;
@@ -175,7 +186,7 @@ bd_status build_graphs(bd_system* h) {
   destroy_graphs(h);
   const KParams p = make_params(h);
   const bool table = h->cfg.normal_mode == BD_NORMALS_TABLE;
-  const Path path = h->diffuse_only() ? Path::kDiffuseOnly : Path::kSorted;
+  const Path path = h->path();
   const bool has_zero = h->Z > 0, has_uni = h->U > 0, has_bim = h->B > 0;
   for (int g = 0; g < 2; g++) {
     const int nsteps = g == 0 ? 1 : kGraphBatch;
@@ -235,6 +246,7 @@ bd_status validate_config(const bd_config* c) {
     if (!(c->box_hi[a] > c->box_lo[a])) return BD_ERR_INVALID_ARGUMENT;
   if (!(c->dt > 0)) return BD_ERR_INVALID_ARGUMENT;
   if (c->normal_mode != BD_NORMALS_BOXMULLER && c->normal_mode != BD_NORMALS_TABLE) return BD_ERR_INVALID_ARGUMENT;
+  if (c->sort_mode > BD_SORT_BINNED) return BD_ERR_INVALID_ARGUMENT;
   return BD_OK;
 }
 
@@ -291,6 +303,7 @@ bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int 
   cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
   h->shape.block_stream = 256;
   h->shape.grid_stream = h->n_sm * 8;
+  h->shape.min_blocks = 1;
   h->shape.block_pairs = 256;
   h->shape.grid_pairs = h->n_sm * 8;
   memset(h->hctrl, 0, sizeof(DevCtrl));
@@ -326,9 +339,12 @@ bd_status grow_particles(bd_system* h, uint64_t cap) {
   DevBuf<uint32_t> best;
   BD_CUDA(s0.alloc(cap));
   BD_CUDA(s1.alloc(cap));
-  BD_CUDA(sc.alloc(cap));
+  if (!h->binned) BD_CUDA(sc.alloc(cap));
   BD_CUDA(best.alloc(cap));
   BD_CUDA(cudaMemsetAsync(best.p, 0xFF, cap * sizeof(uint32_t), h->stream));
+  // cells above 128 records (the large-cell kernel's queue) number at most cap / 129
+  BD_CUDA(h->big.alloc(cap / 129 + 2));
+  BD_CUDA(h->rank_scratch.alloc(cap));
   if (h->have_particles && h->hctrl->n_slots > 0) {
     const float4* src = h->hctrl->cur ? h->state1.p : h->state0.p;
     BD_CUDA(cudaMemcpyAsync(s0.p, src, (size_t)h->hctrl->n_slots * sizeof(float4), cudaMemcpyDeviceToDevice,
@@ -356,12 +372,29 @@ bd_status grow_pairs(bd_system* h, uint32_t cap) {
   return BD_OK;
 }
 
+// The buffer the current sort mode writes: the cell bins (bin_cap records
+// per cell) or the compact scatter buffer (one record per slot).
+bd_status ensure_sort_buffers(bd_system* h, uint32_t K) {
+  if (h->binned) {
+    h->bin_cap = K;
+    const size_t need = (size_t)h->n_cells * K;
+    if (h->bins.n < need) BD_CUDA(h->bins.alloc(need));
+    h->scatter.free();
+  } else {
+    h->bins.free();
+    if (h->capacity > 0 && h->scatter.n < h->capacity) BD_CUDA(h->scatter.alloc(h->capacity));
+  }
+  return BD_OK;
+}
+
 // Grid and Philox key of instance k, planned from its particle count.  An
 // instance keeps its grid for life: the cell grid decides the canonical
 // order, so it must not depend on the other instances.
 void plan_instance(bd_system* h, int k, uint64_t n) {
   DevInstance& D = h->hinst[k];
   choose_grid(h, k, n, &D);
+  if (h->plan_n.size() != h->hinst.size()) h->plan_n.assign(h->hinst.size(), 0);
+  h->plan_n[k] = n;
   D.key_lo = (uint32_t)(h->idesc[k].seed & 0xFFFFFFFFu);
   D.key_hi = (uint32_t)(h->idesc[k].seed >> 32);
   D.block = (uint32_t)k;
@@ -399,7 +432,22 @@ bd_status layout_cells(bd_system* h) {
   BD_CUDA(cudaMemsetAsync(h->cell_start.p, 0, ((size_t)h->n_cells + 1) * sizeof(uint32_t), h->stream));
   BD_CUDA(h->tile_sums.alloc(std::max<uint32_t>(h->n_tiles, 1)));
   BD_CUDA(cudaStreamSynchronize(h->stream));
-  return BD_OK;
+  // Bins hold the planned occupancy of the densest instance with room for
+  // Poisson fluctuations (mean + 7 sd + 8: an overflow at mean 3 has
+  // probability ~1e-14 per cell and step); they only grow.
+  double lam = 0.0;
+  for (int k = 0; k < I; k++) {
+    if (h->server && !h->slot_used[k]) continue;
+    const DevInstance& D = h->hinst[k];
+    const double cells = (double)D.dims[0] * D.dims[1] * D.dims[2];
+    if (k < (int)h->plan_n.size()) lam = std::max(lam, (double)h->plan_n[k] / cells);
+  }
+  uint32_t K = (uint32_t)ceil(lam + 7.0 * sqrt(lam) + 8.0);
+  K = std::max<uint32_t>((K + 3u) & ~3u, h->bin_cap);
+  const uint64_t bytes = (uint64_t)h->n_cells * K * sizeof(float4);
+  const uint32_t mode = h->cfg.sort_mode;
+  h->binned = mode == BD_SORT_BINNED || (mode == BD_SORT_AUTO && bytes <= kBinBudgetBytes);
+  return ensure_sort_buffers(h, K);
 }
 
 bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, const uint64_t* counts) {
@@ -514,6 +562,9 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->state0.free();
   h->state1.free();
   h->scatter.free();
+  h->bins.free();
+  h->big.free();
+  h->rank_scratch.free();
   h->best.free();
   h->cell_count.free();
   h->cell_start.free();
@@ -801,6 +852,21 @@ BD_API bd_status bd_synchronize(bd_handle h) {
         st = grow_particles(h, cap);
         if (st) return st;
       }
+      if (c.status & kStatBins) {
+        // a cell outgrew its bin: larger bins, or the compact sort when
+        // they would not fit the automatic budget
+        uint64_t K = std::max<uint64_t>((uint64_t)c.bin_need + c.bin_need / 4 + 4, (uint64_t)h->bin_cap + 8);
+        K = (K + 3) & ~3ull;
+        const bool fits = (uint64_t)h->n_cells * K * sizeof(float4) <= kBinBudgetBytes;
+        if (K > 0xFFFFFFF0ull || (!fits && h->cfg.sort_mode != BD_SORT_BINNED)) {
+          h->binned = false;
+          st = ensure_sort_buffers(h, h->bin_cap);
+        } else {
+          st = ensure_sort_buffers(h, (uint32_t)K);
+        }
+        if (st) return st;
+        c.bin_need = 0;
+      }
       if (c.status & kStatPairs) {
         uint64_t cap = std::max<uint64_t>(2ull * h->pair_cap, (uint64_t)c.n_pairs + c.n_pairs / 2 + 1024);
         if (cap > 0x7FFFFFFFull) return BD_ERR_CAPACITY;
@@ -811,6 +877,7 @@ BD_API bd_status bd_synchronize(bd_handle h) {
       BD_CUDA(cudaMemsetAsync(h->pending.p, 0, h->pending.n * sizeof(unsigned long long), h->stream));
       c.status = 0;
       c.n_pairs = 0;
+      c.n_big = 0;
       c.n_virtual = 0;
       st = push_ctrl(h);
       if (st) return st;
@@ -1220,7 +1287,7 @@ BD_API bd_status bd_profile_steps(bd_handle h, int nsteps, float* stage_ms, int 
   if (st && st != BD_ERR_EMPTY) return st;
   const KParams p = make_params(h);
   const bool table = h->cfg.normal_mode == BD_NORMALS_TABLE;
-  const Path path = h->diffuse_only() ? Path::kDiffuseOnly : Path::kSorted;
+  const Path path = h->path();
   std::vector<float> acc;
   h->stage_names.clear();
   for (int k = 0; k < nsteps; k++) {
@@ -1258,7 +1325,7 @@ BD_API const char* bd_stage_name(bd_handle h, int k) {
 BD_API bd_status bd_get_kernels_per_step(bd_handle h, int* n) {
   if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
   if (h->diffuse_only()) *n = (h->Z > 0 ? 2 : 0) + 2;
-  else *n = (h->Z > 0 ? 1 : 0) + 7;
+  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 7 : 8);
   return BD_OK;
 }
 
@@ -1360,7 +1427,10 @@ BD_API bd_status bd_set_launch_shape(bd_handle h, int bs, int cs, int bp, int cp
   if (cs < 1 || cs > 64 || cp < 1 || cp > 64) return BD_ERR_INVALID_ARGUMENT;
   h->shape.block_stream = bs;
   h->shape.grid_stream = h->n_sm * cs;
-  h->shape.hi_occupancy = bs == 256 && cs == 6;
+  // a grid of exactly 48 or 32 warps per SM selects the register cap that
+  // keeps all of it resident (40 or 64 registers); other grids run uncapped
+  const int warps = bs / 32 * cs;
+  h->shape.min_blocks = warps == 48 ? 6 : (warps == 32 ? 4 : 1);
   h->shape.block_pairs = bp;
   h->shape.grid_pairs = h->n_sm * cp;
   if (h->host_only || !h->have_particles) return BD_OK;

@@ -209,6 +209,19 @@ __device__ __forceinline__ uint32_t warp_claim(uint32_t* cnt, uint32_t key) {
   return old - 1u - rank;
 }
 
+// Binned sort: lanes with equal keys take consecutive places of their
+// cell's bin with one atomic; the count keeps growing past the bin size so
+// an overflow reports the occupancy it needs.
+__device__ __forceinline__ uint32_t warp_claim_add(uint32_t* cnt, uint32_t key) {
+  const uint32_t peers = __match_any_sync(kFull, key);
+  const int leader = __ffs(peers) - 1;
+  const uint32_t rank = __popc(peers & ((1u << lane_id()) - 1u));
+  uint32_t old = 0;
+  if (key != kNoKey && lane_id() == (uint32_t)leader) old = atomicAdd(&cnt[key], (uint32_t)__popc(peers));
+  old = __shfl_sync(kFull, old, leader);
+  return old + rank;
+}
+
 template <int kThreads>
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
   __shared__ uint32_t warp_sums[kThreads / 32];
@@ -283,8 +296,8 @@ __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
   }
 }
 
-// kMinBlocks = 6 caps registers at 40 for 75% occupancy (a few spills);
-// the launch shape picks the variant.
+// kMinBlocks 4 / 6 cap registers at 64 / 40 (50% / 75% occupancy, the
+// latter with a few spills); the launch shape picks the variant.
 template <bool kTable, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
   const DevCtrl* c = p.ctrl;
@@ -389,6 +402,42 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
   }
 }
 
+// Binned path, pass 1 of 2: advance every record (as k_count) and write it
+// into the next free place of its cell's bin.  Replaces k_count + k_scatter:
+// the step's arithmetic runs once and nothing is recomputed.
+template <bool kTable, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
+  DevCtrl* c = p.ctrl;
+  if (ctrl_status_warp(c)) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  const float4* __restrict__ st = cur_state(p, cur);
+  const uint32_t n_real = ld_u32(&c->n_slots), n_total = n_real + ld_u32(&c->n_virtual);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t K = p.bin_cap;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n_total; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    Out2 o;
+    o.n = 0;
+    if (i < n_real) advance_real<kTable, true>(p, st, i, o);
+    else if (i < n_total) advance_virtual(p, i - n_real, o);
+    const int kmax = __any_sync(kFull, o.n > 1) ? 2 : 1;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (k >= kmax) break;  // warp-uniform
+      const uint32_t key = o.n > k ? o.key[k] : kNoKey;
+      const uint32_t off = warp_claim_add(p.cell_count, key);
+      if (key != kNoKey) {
+        if (off < K) {
+          p.bins[(size_t)key * K + off] = o.r[k];
+        } else {
+          atomicOr(&c->status, kStatBins);
+          atomicMax(&c->bin_need, off + 1u);
+        }
+      }
+    }
+  }
+}
+
 // Position of record r among the records of its cell [s, e) in canonical
 // order; ties between identical records go by slot.
 __device__ __forceinline__ uint32_t canonical_rank(const float4* __restrict__ sc, uint32_t s, uint32_t e,
@@ -422,103 +471,244 @@ __device__ __forceinline__ void emit_pair(const KParams& p, DevCtrl* c, uint32_t
   else atomicOr(&c->status, kStatPairs);
 }
 
-constexpr uint32_t kRankCache = 16;
+// Cells with more records than this are handed from k_pairs_cells to
+// k_pairs_big, which gives each of them a whole CTA.
+constexpr uint32_t kBigCell = 128;
+constexpr int kBigGrid = 304;  // CTAs of k_pairs_big (cells it takes in turn)
 
-// One thread per cell: write the cell's records in canonical order, then
-// test each pair of the cell once and, for members within the largest
-// binding radius of a face, the members of the neighbouring cells.
-template <bool kHasBim>
-__global__ void __launch_bounds__(256) k_pairs(KParams p) {
-  DevCtrl* c = p.ctrl;
-  if (ld_u32(&c->status)) return;
-  const uint32_t cur = ld_u32(&c->cur);
-  float4* __restrict__ nx = next_state(p, cur);
-  const float4* __restrict__ sc = p.scatter;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x; cell < p.n_cells; cell += stride) {
-    const uint32_t s0 = __ldg(&p.cell_start[cell]), e0 = __ldg(&p.cell_start[cell + 1]);
-    if (e0 <= s0) continue;
-    const uint32_t n = e0 - s0;
-    uint32_t rk[kRankCache];
-    for (uint32_t a = 0; a < n; ++a) {
-      const float4 ra = sc[s0 + a];
-      const uint32_t rank = canonical_rank(sc, s0, e0, s0 + a, ra);
-      if (a < kRankCache) rk[a] = rank;
-      // the newborn mark lives only within this step
-      nx[s0 + rank] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
-    }
-    if (!kHasBim) continue;
-    const uint32_t inst = rec_w(sc[s0]) >> 16;  // a cell belongs to one instance
-    if (!advancing(__ldg(&p.inst_flags[inst]))) continue;
-    const DevInstance* __restrict__ Ip = p.inst + inst;
-    const float lo0 = __ldg(&Ip->lo[0]), lo1 = __ldg(&Ip->lo[1]), lo2 = __ldg(&Ip->lo[2]);
-    const float iv0 = __ldg(&Ip->inv[0]), iv1 = __ldg(&Ip->inv[1]), iv2 = __ldg(&Ip->inv[2]);
-    const float cl0 = __ldg(&Ip->cell[0]), cl1 = __ldg(&Ip->cell[1]), cl2 = __ldg(&Ip->cell[2]);
-    const uint32_t d0 = __ldg(&Ip->dims[0]), d1 = __ldg(&Ip->dims[1]), d2 = __ldg(&Ip->dims[2]);
-    const uint32_t cbase = __ldg(&Ip->cell_base), block = __ldg(&Ip->block);
-    const uint32_t local = cell - cbase;
-    const int cx = (int)(local % d0), cy = (int)((local / d0) % d1), cz = (int)(local / (d0 * d1));
-    const float margin = p.prune_margin * fminf(cl0, fminf(cl1, cl2));
-    for (uint32_t a = 0; a < n; ++a) {
-      const float4 ra = sc[s0 + a];
-      const uint32_t wa = rec_w(ra);
-      if (wa & kNewborn) continue;
-      const uint32_t sa = wa & kSpeciesMask;
-      const float max_r = __ldg(&p.species[block * p.S + sa].max_r);
-      if (max_r <= 0.0f) continue;
-      const uint32_t ca = s0 + (a < kRankCache ? rk[a] : canonical_rank(sc, s0, e0, s0 + a, ra));
-      const int32_t* __restrict__ row = p.bim_table + sa * p.S;
-      // pairs inside the cell, each once
-      for (uint32_t bb = a + 1; bb < n; ++bb) {
-        const float4 rb = sc[s0 + bb];
-        const uint32_t wb = rec_w(rb);
-        if (wb & kNewborn) continue;
-        const int32_t b = __ldg(&row[wb & kSpeciesMask]);
-        if (b < 0) continue;
-        const DevBim& br = p.bim[block * p.B + (uint32_t)b];
-        if (dist2(ra, rb) > __ldg(&br.r2)) continue;
-        const uint32_t cb = s0 + (bb < kRankCache ? rk[bb] : canonical_rank(sc, s0, e0, s0 + bb, rb));
-        emit_pair(p, c, min(ca, cb), max(ca, cb), b, __ldg(&br.prob), inst, Ip, cbase);
-      }
-      // neighbour cells across faces closer than the largest binding radius;
-      // the pair is reported from the side with the lower canonical slot
-      const float fx = __fsub_rn(__fmul_rn(__fsub_rn(ra.x, lo0), iv0), (float)cx);
-      const float fy = __fsub_rn(__fmul_rn(__fsub_rn(ra.y, lo1), iv1), (float)cy);
-      const float fz = __fsub_rn(__fmul_rn(__fsub_rn(ra.z, lo2), iv2), (float)cz);
-      const float lox = fx * cl0, hix = (1.0f - fx) * cl0;
-      const float loy = fy * cl1, hiy = (1.0f - fy) * cl1;
-      const float loz = fz * cl2, hiz = (1.0f - fz) * cl2;
-      const float need = max_r + margin, need2 = need * need;
-      const int zlo = (cz > 0 && loz <= need) ? -1 : 0, zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
-      const int ylo = (cy > 0 && loy <= need) ? -1 : 0, yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
-      const int xlo = (cx > 0 && lox <= need) ? -1 : 0, xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
-      if ((zlo | zhi | ylo | yhi | xlo | xhi) == 0) continue;
-      for (int dz = zlo; dz <= zhi; ++dz) {
-        const float ddz = dz < 0 ? loz : (dz > 0 ? hiz : 0.0f);
-        for (int dy = ylo; dy <= yhi; ++dy) {
-          const float ddy = dy < 0 ? loy : (dy > 0 ? hiy : 0.0f);
-          for (int dx = xlo; dx <= xhi; ++dx) {
-            if (dx == 0 && dy == 0 && dz == 0) continue;
-            const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
-            if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
-            const uint32_t nkey =
-                cbase + ((uint32_t)(cz + dz) * d1 + (uint32_t)(cy + dy)) * d0 + (uint32_t)(cx + dx);
-            const uint32_t ns = __ldg(&p.cell_start[nkey]), ne = __ldg(&p.cell_start[nkey + 1]);
-            for (uint32_t m = ns; m < ne; ++m) {
-              const float4 q = sc[m];
-              const uint32_t wq = rec_w(q);
-              if (wq & kNewborn) continue;
-              const int32_t b = __ldg(&row[wq & kSpeciesMask]);
-              if (b < 0) continue;
-              const DevBim& br = p.bim[block * p.B + (uint32_t)b];
-              if (dist2(ra, q) > __ldg(&br.r2)) continue;
-              const uint32_t cq = ns + canonical_rank(sc, ns, ne, m, q);
-              if (ca < cq) emit_pair(p, c, ca, cq, b, __ldg(&br.prob), inst, Ip, cbase);
-            }
-          }
+// First record of a cell: its bin, or its range of the compact scatter buffer.
+template <bool kBinned>
+__device__ __forceinline__ const float4* cell_records(const KParams& p, uint32_t cell, uint32_t cs) {
+  return kBinned ? p.bins + (size_t)cell * p.bin_cap : p.scatter + cs;
+}
+
+// A record looking for partners.
+struct Seeker {
+  float4 r;
+  uint32_t inst, block;
+  float max_r, r2max;
+  const int32_t* row;  // second-order table row of its species
+  const DevInstance* Ip;
+};
+
+// False when the record takes no part in this step's pair search: born in
+// this step, instance not advancing, or a species without second-order
+// reactions.
+__device__ __forceinline__ bool seeker_init(const KParams& p, const float4& r, Seeker& k) {
+  const uint32_t w = rec_w(r);
+  if (w & kNewborn) return false;
+  k.r = r;
+  k.inst = w >> 16;
+  if (!advancing(__ldg(&p.inst_flags[k.inst]))) return false;
+  k.Ip = p.inst + k.inst;
+  k.block = __ldg(&k.Ip->block);
+  const uint32_t sa = w & kSpeciesMask;
+  k.max_r = __ldg(&p.species[k.block * p.S + sa].max_r);
+  // a bound on every squared radius of the species (float rounding of max_r^2)
+  k.r2max = k.max_r * k.max_r * 1.0001f;
+  k.row = p.bim_table + sa * p.S;
+  return k.max_r > 0.0f;
+}
+
+// Local second-order reaction of k with record q when q lies within its
+// binding radius, else -1.
+__device__ __forceinline__ int32_t pair_reaction(const KParams& p, const Seeker& k, const float4& q) {
+  const uint32_t wq = rec_w(q);
+  if (wq & kNewborn) return -1;
+  const float d2 = dist2(k.r, q);
+  if (d2 > k.r2max) return -1;
+  const int32_t b = __ldg(&k.row[wq & kSpeciesMask]);
+  if (b < 0 || d2 > __ldg(&p.bim[k.block * p.B + (uint32_t)b].r2)) return -1;
+  return b;
+}
+
+__device__ __forceinline__ void emit(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t ca, uint32_t cq,
+                                     int32_t b) {
+  emit_pair(p, c, min(ca, cq), max(ca, cq), b, __ldg(&p.bim[k.block * p.B + (uint32_t)b].prob), k.inst, k.Ip,
+            __ldg(&k.Ip->cell_base));
+}
+
+// Pairs of record k (canonical slot ca, in `cell`) with the records of the
+// 13 forward neighbour cells (higher key) whose shared face, edge or corner
+// lies within its largest binding radius.  Every cross-cell pair within
+// range is found from its lower-key side only, so each is tested once.
+template <bool kBinned>
+__device__ void search_forward(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t cell, uint32_t ca) {
+  const DevInstance* __restrict__ Ip = k.Ip;
+  const uint32_t cbase = __ldg(&Ip->cell_base);
+  const float cl0 = __ldg(&Ip->cell[0]), cl1 = __ldg(&Ip->cell[1]), cl2 = __ldg(&Ip->cell[2]);
+  const uint32_t d0 = __ldg(&Ip->dims[0]), d1 = __ldg(&Ip->dims[1]), d2 = __ldg(&Ip->dims[2]);
+  const uint32_t local = cell - cbase;
+  const int cx = (int)(local % d0), cy = (int)((local / d0) % d1), cz = (int)(local / (d0 * d1));
+  const float margin = p.prune_margin * fminf(cl0, fminf(cl1, cl2));
+  const float fx = __fsub_rn(__fmul_rn(__fsub_rn(k.r.x, __ldg(&Ip->lo[0])), __ldg(&Ip->inv[0])), (float)cx);
+  const float fy = __fsub_rn(__fmul_rn(__fsub_rn(k.r.y, __ldg(&Ip->lo[1])), __ldg(&Ip->inv[1])), (float)cy);
+  const float fz = __fsub_rn(__fmul_rn(__fsub_rn(k.r.z, __ldg(&Ip->lo[2])), __ldg(&Ip->inv[2])), (float)cz);
+  const float lox = fx * cl0, hix = (1.0f - fx) * cl0;
+  const float loy = fy * cl1, hiy = (1.0f - fy) * cl1;
+  const float hiz = (1.0f - fz) * cl2;
+  const float need = k.max_r + margin, need2 = need * need;
+  const int zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
+  const int ylo = (cy > 0 && loy <= need) ? -1 : 0, yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
+  const int xlo = (cx > 0 && lox <= need) ? -1 : 0, xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
+  if ((zhi | yhi | xhi) == 0) return;
+  for (int dz = 0; dz <= zhi; ++dz) {
+    const float ddz = dz > 0 ? hiz : 0.0f;
+    for (int dy = (dz > 0 ? ylo : 0); dy <= yhi; ++dy) {
+      const float ddy = dy < 0 ? loy : (dy > 0 ? hiy : 0.0f);
+      for (int dx = (dz > 0 || dy > 0 ? xlo : 1); dx <= xhi; ++dx) {
+        const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
+        if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
+        const uint32_t nkey = cbase + ((uint32_t)(cz + dz) * d1 + (uint32_t)(cy + dy)) * d0 + (uint32_t)(cx + dx);
+        const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
+        const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
+        for (uint32_t m = 0; m < nn; ++m) {
+          const float4 q = __ldg(&nb[m]);
+          const int32_t b = pair_reaction(p, k, q);
+          if (b >= 0) emit(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
         }
       }
     }
+  }
+}
+
+// Canonical order + pair search, one warp per 32 consecutive cells.  The
+// warp walks the cells' records 32 at a time (lane t of a round = record t
+// of the cells' concatenation), so each lane handles one record whatever
+// the cell sizes.  For its record a lane
+//   * counts the records of the cell that precede it in canonical order and
+//     writes it to cell_start[cell] + that rank in the next state;
+//   * in the same loop, tests the cell's later records (storage order)
+//     against its binding radii, each in-cell pair once;
+//   * searches the forward neighbour cells (search_forward).
+// Canonical slots of partners are computed only for pairs within range.
+// Cells above kBigCell records are queued for k_pairs_big.  kBinned: the
+// records come from the cell bins, whose counts are cleared here for the
+// next step; otherwise from the compact scatter buffer.
+template <bool kHasBim, bool kBinned>
+__global__ void __launch_bounds__(256) k_pairs_cells(KParams p) {
+  __shared__ uint32_t s_cell[8][32], s_cs[8][32], s_n[8][32], s_off[8][32];
+  DevCtrl* c = p.ctrl;
+  if (ctrl_status_warp(c)) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  float4* __restrict__ nx = next_state(p, cur);
+  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  const uint32_t n_tasks = (p.n_cells + 31u) >> 5;
+  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  const uint32_t le_mask = lane == 31 ? kFull : ((2u << lane) - 1u);
+  for (uint32_t task = blockIdx.x * (blockDim.x >> 5) + warp; task < n_tasks; task += nw) {
+    const uint32_t cell = task * 32u + lane;
+    uint32_t cs = 0, n = 0;
+    if (cell < p.n_cells) {
+      cs = __ldg(&p.cell_start[cell]);
+      n = __ldg(&p.cell_start[cell + 1]) - cs;
+      if (kBinned) p.cell_count[cell] = 0u;
+      if (n > kBigCell) {
+        const uint32_t b = atomicAdd(&c->n_big, 1u);
+        if (b < p.big_cap) p.big[b] = cell;
+        else atomicOr(&c->status, kStatBounds);
+        n = 0;
+      }
+    }
+    const uint32_t q = __popc(__ballot_sync(kFull, n > 0) & ((1u << lane) - 1u));
+    uint32_t incl = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(kFull, incl, d);
+      if (lane >= (uint32_t)d) incl += t;
+    }
+    const uint32_t off = incl - n, total = __shfl_sync(kFull, incl, 31);
+    if (n > 0) {
+      s_cell[warp][q] = cell;
+      s_cs[warp][q] = cs;
+      s_n[warp][q] = n;
+      s_off[warp][q] = off;
+    }
+    __syncwarp();
+    uint32_t before = 0;  // non-empty cells that start before this round
+    for (uint32_t rb = 0; rb < total; rb += 32u) {
+      const uint32_t M = __reduce_or_sync(kFull, (n > 0 && off >= rb && off - rb < 32u) ? 1u << (off - rb) : 0u);
+      const uint32_t t = rb + lane;
+      if (t < total) {
+        const uint32_t oq = before + __popc(M & le_mask) - 1u;
+        const uint32_t ocell = s_cell[warp][oq], ocs = s_cs[warp][oq], on = s_n[warp][oq];
+        const uint32_t j = t - s_off[warp][oq];
+        const float4* __restrict__ cb = cell_records<kBinned>(p, ocell, ocs);
+        const float4 ra = __ldg(&cb[j]);
+        Seeker k;
+        const bool search = kHasBim && seeker_init(p, ra, k);
+        uint32_t rank = 0, cand = 0;  // cand: bit m = later member m < 32 within range
+        for (uint32_t m = 0; m < on; ++m) {
+          const float4 qm = __ldg(&cb[m]);
+          rank += (rec_less(qm, ra) || (m < j && rec_equal(qm, ra))) ? 1u : 0u;
+          if (search && m > j && m < 32u && pair_reaction(p, k, qm) >= 0) cand |= 1u << m;
+        }
+        const uint32_t ca = ocs + rank;
+        if (ca < p.capacity) nx[ca] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
+        else atomicOr(&c->status, kStatBounds);
+        if (search) {
+          while (cand) {
+            const uint32_t m = (uint32_t)(__ffs(cand) - 1);
+            cand &= cand - 1u;
+            const float4 qm = __ldg(&cb[m]);
+            emit(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), pair_reaction(p, k, qm));
+          }
+          for (uint32_t m = max(j + 1u, 32u); m < on; ++m) {  // cells of 33..kBigCell records
+            const float4 qm = __ldg(&cb[m]);
+            const int32_t b = pair_reaction(p, k, qm);
+            if (b >= 0) emit(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), b);
+          }
+          search_forward<kBinned>(p, c, k, ocell, ca);
+        }
+      }
+      before += __popc(M);
+    }
+    __syncwarp();
+  }
+}
+
+// Cells queued by k_pairs_cells (more than kBigCell records, e.g. particles
+// released at one point), one CTA per cell: ranks first (kept in
+// rank_scratch by storage position), then the pairs, which read the
+// partners' ranks instead of recounting them.
+template <bool kHasBim, bool kBinned>
+__global__ void __launch_bounds__(256) k_pairs_big(KParams p) {
+  __shared__ uint32_t s_stop;
+  DevCtrl* c = p.ctrl;
+  if (threadIdx.x == 0) s_stop = ld_u32(&c->status);
+  __syncthreads();
+  if (s_stop) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  float4* __restrict__ nx = next_state(p, cur);
+  const uint32_t nbig = min(ld_u32(&c->n_big), p.big_cap);
+  for (uint32_t bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
+    const uint32_t cell = p.big[bi];
+    const uint32_t cs = p.cell_start[cell], n = p.cell_start[cell + 1] - cs;
+    const float4* __restrict__ cb = cell_records<kBinned>(p, cell, cs);
+    for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+      const float4 ra = cb[t];
+      const uint32_t rank = canonical_rank(cb, 0, n, t, ra);
+      if (cs + t < p.capacity && cs + rank < p.capacity) {
+        p.rank_scratch[cs + t] = rank;
+        nx[cs + rank] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
+      } else {
+        atomicOr(&c->status, kStatBounds);
+      }
+    }
+    __syncthreads();
+    if (kHasBim) {
+      for (uint32_t t = threadIdx.x; t < n && cs + n <= p.capacity; t += blockDim.x) {
+        Seeker k;
+        if (!seeker_init(p, cb[t], k)) continue;
+        const uint32_t ca = cs + p.rank_scratch[cs + t];
+        for (uint32_t m = t + 1; m < n; ++m) {
+          const int32_t b = pair_reaction(p, k, cb[m]);
+          if (b >= 0) emit(p, c, k, ca, cs + p.rank_scratch[cs + m], b);
+        }
+        search_forward<kBinned>(p, c, k, cell, ca);
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -645,6 +835,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
   if (threadIdx.x == 0) {
     c->n_pairs_last = K;
     c->n_pairs = 0;
+    c->n_big = 0;
     c->deaths_last = s_deaths;
     c->n_slots = c->n_sorted;
     c->n_virtual = 0;
@@ -763,14 +954,44 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     done("k_finalize_inplace");
     return n;
   }
-  const bool hi_occ = shape.hi_occupancy;
-  if (table) {
-    if (hi_occ) k_count<true, 6><<<gs, bs, 0, s>>>(p);
-    else k_count<true, 1><<<gs, bs, 0, s>>>(p);
-  } else {
-    if (hi_occ) k_count<false, 6><<<gs, bs, 0, s>>>(p);
-    else k_count<false, 1><<<gs, bs, 0, s>>>(p);
+  // Register-capped variants of the streaming kernels, picked by the launch
+  // shape's resident CTAs per SM: 1 = no cap, 4 = 64 registers, 6 = 40.
+#define BD_STREAM_LAUNCH(KERNEL)                                   \
+  do {                                                             \
+    switch (shape.min_blocks) {                                    \
+      case 6:                                                      \
+        if (table) KERNEL<true, 6><<<gs, bs, 0, s>>>(p);           \
+        else KERNEL<false, 6><<<gs, bs, 0, s>>>(p);                \
+        break;                                                     \
+      case 4:                                                      \
+        if (table) KERNEL<true, 4><<<gs, bs, 0, s>>>(p);           \
+        else KERNEL<false, 4><<<gs, bs, 0, s>>>(p);                \
+        break;                                                     \
+      default:                                                     \
+        if (table) KERNEL<true, 1><<<gs, bs, 0, s>>>(p);           \
+        else KERNEL<false, 1><<<gs, bs, 0, s>>>(p);                \
+    }                                                              \
+  } while (0)
+  if (path == Path::kBinned) {
+    BD_STREAM_LAUNCH(k_bin);
+    done("k_bin");
+    k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
+    done("k_scan_tiles");
+    k_scan_top<<<1, 1024, 0, s>>>(p);
+    done("k_scan_top");
+    k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
+    done("k_scan_down");
+    if (has_bim) k_pairs_cells<true, true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+    else k_pairs_cells<false, true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+    done("k_pairs_cells");
+    if (has_bim) k_pairs_big<true, true><<<kBigGrid, 256, 0, s>>>(p);
+    else k_pairs_big<false, true><<<kBigGrid, 256, 0, s>>>(p);
+    done("k_pairs_big");
+    k_match<<<1, 1024, 0, s>>>(p);
+    done("k_match");
+    return n;
   }
+  BD_STREAM_LAUNCH(k_count);
   done("k_count");
   k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
   done("k_scan_tiles");
@@ -778,17 +999,15 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   done("k_scan_top");
   k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
   done("k_scan_down");
-  if (table) {
-    if (hi_occ) k_scatter<true, 6><<<gs, bs, 0, s>>>(p);
-    else k_scatter<true, 1><<<gs, bs, 0, s>>>(p);
-  } else {
-    if (hi_occ) k_scatter<false, 6><<<gs, bs, 0, s>>>(p);
-    else k_scatter<false, 1><<<gs, bs, 0, s>>>(p);
-  }
+  BD_STREAM_LAUNCH(k_scatter);
+#undef BD_STREAM_LAUNCH
   done("k_scatter");
-  if (has_bim) k_pairs<true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
-  else k_pairs<false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
-  done("k_pairs");
+  if (has_bim) k_pairs_cells<true, false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+  else k_pairs_cells<false, false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+  done("k_pairs_cells");
+  if (has_bim) k_pairs_big<true, false><<<kBigGrid, 256, 0, s>>>(p);
+  else k_pairs_big<false, false><<<kBigGrid, 256, 0, s>>>(p);
+  done("k_pairs_big");
   k_match<<<1, 1024, 0, s>>>(p);
   done("k_match");
   return n;

@@ -10,7 +10,8 @@ namespace bd {
 // Everything a step kernel reads or writes, passed by value.
 struct KParams {
   float4* state[2];           // ping-pong state buffers, DevCtrl::cur selects
-  float4* scatter;            // cell-ordered staging buffer of the sort
+  float4* scatter;            // cell-ordered staging buffer of the compact sort
+  float4* bins;               // [n_cells][bin_cap] records per cell (binned sort)
   DevCtrl* ctrl;
   const DevInstance* inst;
   const DevSpecies* species;  // [block][S]
@@ -35,16 +36,24 @@ struct KParams {
   uint32_t n_inst, S, U, B, Z, R;
   uint32_t n_cells, n_tiles;
   uint32_t capacity, pair_cap;
+  uint32_t bin_cap;           // records per cell bin (binned sort)
+  uint32_t* big;              // [big_cap] cells queued for k_pairs_big
+  uint32_t* rank_scratch;     // [capacity] canonical ranks inside queued cells
+  uint32_t big_cap;
   float prune_margin;         // fraction of a cell edge added to pruning distances
 };
 
-enum class Path { kDiffuseOnly, kSorted };
+// kSorted: counting sort into compact cell ranges (k_count, scans,
+// k_scatter) before the pair kernel.  kBinned: each record goes straight
+// into a fixed-size bin of its cell (k_bin), the scans give the compact
+// output ranges and the pair kernel reads the bins.  Same results.
+enum class Path { kDiffuseOnly, kSorted, kBinned };
 
 struct LaunchShape {
   int grid_stream;            // blocks of the grid-stride particle kernels
   int block_stream;           // threads per block of those kernels
   int grid_pairs, block_pairs;
-  bool hi_occupancy;          // 40-register variants of k_count / k_scatter (6 CTAs/SM)
+  int min_blocks;             // register-capped streaming kernels: 1 (none), 4 (64 regs), 6 (40 regs)
 };
 
 // Called after each kernel of a step is enqueued (stage name); lets the

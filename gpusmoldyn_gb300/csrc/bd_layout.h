@@ -106,7 +106,9 @@ struct DevCtrl {
   uint32_t steps_done;     // completed steps since the last host reset
   uint64_t step;           // global step counter
   uint32_t deaths_last;    // bimolecular deaths of the last step
-  uint32_t pad[5];
+  uint32_t bin_need;       // largest cell occupancy seen by a bin that overflowed
+  uint32_t n_big;          // cells queued for the large-cell pair kernel
+  uint32_t pad[3];
 };
 
 enum StatusBits : uint32_t {
@@ -114,6 +116,7 @@ enum StatusBits : uint32_t {
   kStatPairs = 2u,         // candidate pairs exceed the pair capacity
   kStatBounds = 4u,        // a device-side bounds check failed
   kStatTimeout = 8u,       // a bounded wait ran out
+  kStatBins = 16u,         // a cell held more records than its bin
 };
 
 // Pair list entry written by the pair kernel and resolved by the matcher.

@@ -16,7 +16,7 @@ import time
 
 import numpy as np
 
-from .configs import c3_network, c3_zeroth_rate, rng, uniform_positions
+from .configs import c3_add_network, c3_network, c3_species, c3_steady_state, rng, uniform_positions
 from .system import System
 
 # device bytes per particle slot: two state buffers + the sort staging buffer
@@ -32,19 +32,12 @@ def c3_request(job, density=2.0):
     desc = dict(box_lo=(0.0, 0.0, 0.0), box_hi=(side, side, side), seed=job["seed"])
     g = rng(job["seed"])
     pos = uniform_positions(g, n, desc["box_lo"], desc["box_hi"])
-    sp = (np.arange(n) % 8).astype(np.int32)
-    return desc, pos, sp, job["steps"]
+    _, frac = c3_steady_state(c3_network()[1], density)
+    return desc, pos, c3_species(n, frac), job["steps"]
 
 
 def c3_server_network(s, density=2.0, network_seed=3):
-    D, rx = c3_network(network_seed)
-    for d in D:
-        s.add_species(float(d))
-    z = c3_zeroth_rate(D, rx, density)
-    s.add_reaction(0, [], [0], z)
-    s.add_reaction(0, [], [1], z)
-    for order, rc, pr, k in rx:
-        s.add_reaction(order, rc, pr, float(k))
+    c3_add_network(s, density, network_seed)
     s.finalize()
 
 

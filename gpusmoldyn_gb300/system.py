@@ -17,10 +17,12 @@ class System:
 
     ``instances`` (list of dicts with box_lo, box_hi, seed, d_scale, k2_scale,
     cell_size) makes an ensemble of independent instances sharing the
-    species and reaction network."""
+    species and reaction network.  ``sort`` picks how records reach their
+    cells ("auto", "compact" or "binned"; identical results)."""
 
     def __init__(self, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), dt=1e-3, seed=1, normals="boxmuller",
-                 capacity=0, cell_size=0.0, cell_occupancy=0.0, pair_capacity=0, device=0, instances=None):
+                 capacity=0, cell_size=0.0, cell_occupancy=0.0, pair_capacity=0, device=0, instances=None,
+                 sort="auto"):
         self.lib = L.load()
         self.server = False
         cfg = L.bd_config()
@@ -36,6 +38,7 @@ class System:
         cfg.pair_capacity = int(pair_capacity)
         cfg.device = device
         cfg.normal_mode = L.BD_NORMALS_TABLE if normals == "table" else L.BD_NORMALS_BOXMULLER
+        cfg.sort_mode = {"auto": L.BD_SORT_AUTO, "compact": L.BD_SORT_COMPACT, "binned": L.BD_SORT_BINNED}[sort]
         self.cfg = cfg
         self.dt = dt
         self.h = C.c_void_p()

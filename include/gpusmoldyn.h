@@ -75,6 +75,17 @@ enum {
   BD_PP_OFFSET0 = 4      /* products exactly at the reaction point (b = 0) */
 };
 
+/* bd_config.sort_mode.  Both modes give identical results (records in
+ * canonical cell order, same pairs); they differ in memory and speed.
+ * BINNED writes each advanced record straight into a fixed-size bin of its
+ * cell (bins sized from the planned occupancy, grown and the step replayed
+ * when one overflows) and needs n_cells x bin size x 16 bytes.  COMPACT
+ * counts, scans and scatters into exact cell ranges (the reference's
+ * calcHash + RadixSort + reorderDataAndFindCellStart in one counting sort)
+ * and needs 16 bytes per slot.  AUTO takes BINNED while its bins fit in
+ * 32 GiB. */
+enum { BD_SORT_AUTO = 0, BD_SORT_COMPACT = 1, BD_SORT_BINNED = 2 };
+
 typedef struct bd_config {
   float box_lo[3];           /* reflecting box, replaces the fixed [-1,1]^3 world */
   float box_hi[3];           /* (particleSystem.cpp:73, particleSystem.h:114-120) */
@@ -86,7 +97,8 @@ typedef struct bd_config {
   int normal_mode;           /* BD_NORMALS_* */
   int device;                /* CUDA device ordinal */
   uint32_t pair_capacity;    /* candidate-pair list length; 0 = automatic */
-  uint32_t reserved[7];
+  uint32_t sort_mode;        /* BD_SORT_*: how records reach their cells */
+  uint32_t reserved[6];
 } bd_config;
 
 /* Derived parameters of one reaction, as the reference stores them in its
@@ -239,7 +251,9 @@ BD_API bd_status bd_get_species_d(bd_handle h, int instance, int species, float 
 BD_API bd_status bd_set_cell_size(bd_handle h, float cell_size);
 /* Launch shape of the particle kernels (autotuner): threads per CTA (a
  * multiple of 32, at most 256) and CTAs per SM of the grid-stride grids, for
- * the streaming kernels and for the pair kernel.  The result of a step does
+ * the streaming kernels and for the pair kernel.  A streaming grid of
+ * exactly 48 or 32 warps per SM runs register-capped kernel variants (40 or
+ * 64 registers) so that all of it is resident.  The result of a step does
  * not depend on it. */
 BD_API bd_status bd_set_launch_shape(bd_handle h, int block_stream, int ctas_per_sm_stream, int block_pairs,
                                      int ctas_per_sm_pairs);

@@ -69,9 +69,13 @@ def dense_a_b(n_a, n_b, side, seed, normals="table", kon=0.01, **kw):
     return s
 
 
-def test_irreversible_c1_shape_bit_exact():
+SORTS = ["binned", "compact"]
+
+
+@pytest.mark.parametrize("sort", SORTS)
+def test_irreversible_c1_shape_bit_exact(sort):
     # c1 at a higher rate so that each step has reactions and contested pairs
-    s = dense_a_b(2000, 2000, 2.0, seed=11, kon=5.0)
+    s = dense_a_b(2000, 2000, 2.0, seed=11, kon=5.0, sort=sort)
     _, npairs, ev = run_parity(s, 25)
     assert npairs > 100 and ev[0] > 100
 
@@ -125,10 +129,11 @@ def test_reversible_with_offsets_bit_exact():
     assert ev[0] > 20 and ev[1] > 20
 
 
-def test_mixed_network_bit_exact():
+@pytest.mark.parametrize("sort", SORTS)
+def test_mixed_network_bit_exact(sort):
     # zeroth-order births (one and two products), decay, conversion, a
     # displaced two-product birth, a homodimer and a two-product pair reaction
-    s = System((0, 0, 0), (3.0, 2.0, 2.5), dt=1e-3, seed=15, normals="table")
+    s = System((0, 0, 0), (3.0, 2.0, 2.5), dt=1e-3, seed=15, normals="table", sort=sort)
     for d in (0.7, 0.3, 2.0, 0.1, 1.2):
         s.add_species(d)
     s.add_reaction(0, [], [0], 300.0)
@@ -175,11 +180,12 @@ def test_graph_batches_equal_single_steps():
     assert a.step_count() == b.step_count() == 19
 
 
-def test_capacity_growth_replays_exactly():
+@pytest.mark.parametrize("sort", SORTS)
+def test_capacity_growth_replays_exactly(sort):
     """Births overflow a tight capacity: the step is replayed after the
     buffers grow, giving the same result as a roomy run."""
     def make(cap):
-        s = System((0, 0, 0), (2, 2, 2), dt=1e-3, seed=18, normals="table", capacity=cap)
+        s = System((0, 0, 0), (2, 2, 2), dt=1e-3, seed=18, normals="table", capacity=cap, sort=sort)
         s.add_species(1.0)
         s.add_species(1.0)
         s.add_reaction(1, [0], [0, 1], 50.0)   # ~5% of the A give birth every step
@@ -206,7 +212,8 @@ def test_pair_capacity_growth_replays_exactly():
     np.testing.assert_array_equal(gpu_records(a), gpu_records(b))
 
 
-def test_ensemble_instances_match_oracle_alone():
+@pytest.mark.parametrize("sort", SORTS)
+def test_ensemble_instances_match_oracle_alone(sort):
     """Each instance of a batched ensemble evolves exactly as the oracle runs
     it alone: RNG keys, cells and slots are instance-local."""
     inst = []
@@ -215,7 +222,7 @@ def test_ensemble_instances_match_oracle_alone():
         side = float((n / 1500.0) ** (1 / 3))
         inst.append(dict(box_lo=(0.0, 0.0, 0.0), box_hi=(side, side, side), seed=100 + k,
                          d_scale=[0.5, 1.0, 2.0, 1.5][k], k2_scale=[1.0, 2.0, 0.5, 3.0][k]))
-    s = System(dt=1e-3, seed=1, normals="table", instances=inst)
+    s = System(dt=1e-3, seed=1, normals="table", instances=inst, sort=sort)
     A, B, Cc = s.add_species(1.0), s.add_species(1.0), s.add_species(0.5)
     s.add_reaction(2, [A, B], [Cc], 3.0)
     u = s.add_reaction(1, [Cc], [A, B], 50.0)
@@ -242,3 +249,26 @@ def test_ensemble_instances_match_oracle_alone():
             np.testing.assert_array_equal(mine, live, err_msg=f"instance {k} step {t}")
     np.testing.assert_array_equal(s.instance_counts(),
                                   [int(np.sum(r[:, 3] != 0xFFFFFFFF)) for r in recs])
+
+
+def test_bin_overflow_grows_and_replays_exactly():
+    """A cluster far denser than the planned occupancy overflows the cell
+    bins: the bins grow, the step is replayed, and the result equals the
+    oracle's and the compact sort's."""
+    def make(sort):
+        s = System((0, 0, 0), (2.0, 2.0, 2.0), dt=1e-3, seed=21, normals="table", sort=sort)
+        A, B, Cc = s.add_species(0.2), s.add_species(0.2), s.add_species(0.1)
+        s.add_reaction(2, [A, B], [Cc], 1.0)
+        s.finalize()
+        g = rng(21)
+        pos = uniform_positions(g, 6000, (0, 0, 0), (2.0, 2.0, 2.0))
+        pos[:600] = uniform_positions(g, 600, (0.9, 0.9, 0.9), (0.95, 0.95, 0.95))  # one cell's worth x 200
+        s.set_particles(pos, (np.arange(6000) % 2).astype(np.int32))
+        return s
+    binned, compact = make("binned"), make("compact")
+    _, npairs, ev = run_parity(binned, 6)
+    assert npairs > 0 and ev[0] > 0
+    compact.step(6)
+    compact.synchronize()
+    np.testing.assert_array_equal(gpu_records(binned), gpu_records(compact))
+    assert np.diff(binned.cells()).max() > 100
