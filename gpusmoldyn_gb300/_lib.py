@@ -112,6 +112,8 @@ _SIGS = {
     "bd_instance_poll": (C.c_int, [H, P, C.c_int, C.POINTER(C.c_int)]),
     "bd_instance_harvest": (C.c_int, [H, C.c_int, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_instance_state": (C.c_int, [H, C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "bd_cell_sort_static": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                      C.POINTER(C.c_uint32), P, P, P]),
     "bd_numrxnrate": (C.c_double, [C.c_double, C.c_double, C.c_double]),
     "bd_actrxnrate": (C.c_double, [C.c_double, C.c_double]),
     "bd_bindingradius": (C.c_double, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),

@@ -311,6 +311,26 @@ BD_API bd_status bd_instance_harvest(bd_handle h, int slot, float *xyz4, int *sp
 /* Steps taken by the instance in a slot and its flags (1 active, 2 frozen). */
 BD_API bd_status bd_instance_state(bd_handle h, int slot, uint32_t *steps, uint32_t *flags);
 
+/* ------------------------------------------------- allocation-free sort */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * -- a host application that owns all device memory and forbids its
+ * plugins to grow the footprint, or a time-critical loop that cannot afford
+ * cudaMalloc's implicit device synchronisation -- this sorts n records
+ * (device float4 x, y, z, w) into the uniform grid of `dims` cells over the
+ * box, exactly as a step orders its state: by cell, then by record bits
+ * inside a cell.  d_out receives the n sorted records and d_cell_start the
+ * n_cells + 1 cell starts; both are the caller's device buffers, and the
+ * call is enqueued on `stream` (a cudaStream_t; NULL = legacy default).
+ * Nothing is allocated: the per-cell counts and scan partials live in one
+ * file-scope device array of 2^20 + 256 words (about 4 MiB) that every GPU
+ * loading the library keeps until the process exits.  More than 2^20 cells
+ * returns BD_ERR_CAPACITY.  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress), so make the first call before any
+ * stream capture.  Calls share the array and each clears its counts first;
+ * calls that overlap on the GPU race on it and must be serialised. */
+BD_API bd_status bd_cell_sort_static(const float *d_in, uint64_t n, const float box_lo[3], const float box_hi[3],
+                                     const uint32_t dims[3], float *d_out, uint32_t *d_cell_start, void *stream);
+
 /* ------------------------------------------------------ rxnparam (host) */
 /* Restatements of rxnparam.h:39-42 (Andrews-Bray rate tables, rxnparam.cpp:
  * 42-308): rate per step in length^3, binding radius, unbinding radius. */
