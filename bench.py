@@ -191,6 +191,16 @@ def algorithmic_bytes(kernel, n_in, n_out, n_cells, binned=True):
 
 
 # -------------------------------------------------------------- workloads
+def workload_desc(name, n_override=0):
+    if name == "c3":
+        n = n_override or 16_000_000
+        side = 200.0 * (n / 16_000_000) ** (1 / 3)
+        return f"c3: {n} particles, 8 species, 12 reactions, {side:.1f} um reflecting cube, dt 1 ms"
+    n = n_override or 1_000_000
+    side = 60.0 * (n / 1_000_000) ** (1 / 3)
+    return f"c2: {n} particles, A+B<->C, {side:.1f} um cube, dt 0.5 ms"
+
+
 def build_workload(name, n_override=0, normals="boxmuller", device=0, host_only=False):
     from gpusmoldyn_gb300 import configs
 
@@ -198,12 +208,11 @@ def build_workload(name, n_override=0, normals="boxmuller", device=0, host_only=
     if name == "c3":
         n = n_override or 16_000_000
         side = 200.0 * (n / 16_000_000) ** (1 / 3)
-        return configs.build_c3(n=n, side=side, normals=normals, device=dev), f"c3: {n} particles, 8 species, " \
-            f"12 reactions, {side:.1f} um reflecting cube, dt 1 ms"
+        return configs.build_c3(n=n, side=side, normals=normals, device=dev), workload_desc(name, n)
     n = n_override or 1_000_000
     side = 60.0 * (n / 1_000_000) ** (1 / 3)
     return configs.build_c2(n_a=n // 2, n_b=n - n // 2, side=side, normals=normals, device=dev), \
-        f"c2: {n} particles, A+B<->C, {side:.1f} um cube, dt 0.5 ms"
+        workload_desc(name, n)
 
 
 def network_and_particles(name, n_override, device):
@@ -273,7 +282,8 @@ def run_reference(args, dist):
         "steps": done, "warmup": max(args.warmup, 1), "ms_per_step": el / max(done, 1) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Philox uniform positions)",
-        "config": {"workload": "c3 network, sampled (see cpu_baseline.sample)", "parallelism": "cpu"},
+        "config": {"workload": workload_desc("c3", args.n), "parallelism": f"cpu, {threads} threads",
+                   "sampled": "each step is a bounded sample of the workload (cpu_baseline.sample)"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

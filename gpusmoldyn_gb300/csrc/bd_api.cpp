@@ -95,7 +95,8 @@ struct bd_system {
   DevBuf<uint32_t> inst_step, inst_slot_base, zero_off;
   DevBuf<unsigned long long> events, pending;
   DevBuf<float4> state0, state1, scatter, bins;
-  DevBuf<uint32_t> best, cell_count, cell_start, tile_sums, big, rank_scratch;
+  DevBuf<uint32_t> best, cell_count, cell_start, tile_sums, big;
+  DevBuf<float4> big_scratch;  // allocated when a cell first outgrows the pair kernel
   DevBuf<DevPair> pairs;
 
   std::vector<DevInstance> hinst;
@@ -145,10 +146,12 @@ KParams make_params(bd_system* h) {
   p.bins = h->bins.p;
   p.bin_cap = h->bin_cap;
   p.big = h->big.p;
-  p.rank_scratch = h->rank_scratch.p;
+  p.big_scratch = h->big_scratch.p;
   p.big_cap = (uint32_t)h->big.n;
+  p.big_scratch_cap = (uint32_t)h->big_scratch.n;
   p.ctrl = h->ctrl.p;
   p.inst = h->dinst.p;
+  if (!h->hinst.empty()) p.inst0 = h->hinst[0];
   p.species = h->dspecies.p;
   p.uni = h->duni.p;
   p.bim = h->dbim.p;
@@ -301,9 +304,11 @@ bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int 
     return BD_ERR_CUDA;
   }
   cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, h->device);
+  // 4 resident CTAs of 256 threads per SM with the 64-register variants
+  // (measured on the 16M c3 step: 0.90 ms against 1.00 ms uncapped)
   h->shape.block_stream = 256;
-  h->shape.grid_stream = h->n_sm * 8;
-  h->shape.min_blocks = 1;
+  h->shape.grid_stream = h->n_sm * 4;
+  h->shape.min_blocks = 4;
   h->shape.block_pairs = 256;
   h->shape.grid_pairs = h->n_sm * 8;
   memset(h->hctrl, 0, sizeof(DevCtrl));
@@ -344,7 +349,7 @@ bd_status grow_particles(bd_system* h, uint64_t cap) {
   BD_CUDA(cudaMemsetAsync(best.p, 0xFF, cap * sizeof(uint32_t), h->stream));
   // cells above 128 records (the large-cell kernel's queue) number at most cap / 129
   BD_CUDA(h->big.alloc(cap / 129 + 2));
-  BD_CUDA(h->rank_scratch.alloc(cap));
+  if (h->big_scratch.n) BD_CUDA(h->big_scratch.alloc(cap));
   if (h->have_particles && h->hctrl->n_slots > 0) {
     const float4* src = h->hctrl->cur ? h->state1.p : h->state0.p;
     BD_CUDA(cudaMemcpyAsync(s0.p, src, (size_t)h->hctrl->n_slots * sizeof(float4), cudaMemcpyDeviceToDevice,
@@ -564,7 +569,7 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->scatter.free();
   h->bins.free();
   h->big.free();
-  h->rank_scratch.free();
+  h->big_scratch.free();
   h->best.free();
   h->cell_count.free();
   h->cell_start.free();
@@ -867,6 +872,7 @@ BD_API bd_status bd_synchronize(bd_handle h) {
         if (st) return st;
         c.bin_need = 0;
       }
+      if (c.status & kStatScratch) BD_CUDA(h->big_scratch.alloc(h->capacity));
       if (c.status & kStatPairs) {
         uint64_t cap = std::max<uint64_t>(2ull * h->pair_cap, (uint64_t)c.n_pairs + c.n_pairs / 2 + 1024);
         if (cap > 0x7FFFFFFFull) return BD_ERR_CAPACITY;
@@ -996,6 +1002,51 @@ BD_API bd_status bd_create_server(const bd_config* cfg, int max_instances, bd_ha
 }
 
 namespace {
+
+// Records in the order a sort of one step leaves them: by cell key (the
+// device's cell_key, the same correctly rounded float operations), then by
+// the record's words as unsigned integers.  Empty slots go last.
+void canonical_sort(const DevInstance& I, std::vector<float4>* recs) {
+  struct Keyed {
+    uint32_t key, x, y, z, w;
+  };
+  std::vector<Keyed> v(recs->size());
+  for (size_t i = 0; i < recs->size(); i++) {
+    const float4 q = (*recs)[i];
+    Keyed& e = v[i];
+    memcpy(&e.x, &q.x, 4);
+    memcpy(&e.y, &q.y, 4);
+    memcpy(&e.z, &q.z, 4);
+    memcpy(&e.w, &q.w, 4);
+    if (e.w == kDead) {
+      e.key = 0xFFFFFFFFu;
+      continue;
+    }
+    const float xyz[3] = {q.x, q.y, q.z};
+    uint32_t c[3];
+    for (int a = 0; a < 3; a++) {
+      const float f = (xyz[a] - I.lo[a]) * I.inv[a];
+      int ci = (int)floorf(f);
+      ci = ci < 0 ? 0 : (ci > (int)I.dims[a] - 1 ? (int)I.dims[a] - 1 : ci);
+      c[a] = (uint32_t)ci;
+    }
+    e.key = (c[2] * I.dims[1] + c[1]) * I.dims[0] + c[0];
+  }
+  std::sort(v.begin(), v.end(), [](const Keyed& a, const Keyed& b) {
+    if (a.key != b.key) return a.key < b.key;
+    if (a.x != b.x) return a.x < b.x;
+    if (a.y != b.y) return a.y < b.y;
+    if (a.z != b.z) return a.z < b.z;
+    return a.w < b.w;
+  });
+  for (size_t i = 0; i < v.size(); i++) {
+    float4& q = (*recs)[i];
+    memcpy(&q.x, &v[i].x, 4);
+    memcpy(&q.y, &v[i].y, 4);
+    memcpy(&q.z, &v[i].z, 4);
+    memcpy(&q.w, &v[i].w, 4);
+  }
+}
 
 // Slots whose instance was harvested become free once a step has dropped
 // its records.
@@ -1162,6 +1213,11 @@ BD_API bd_status bd_instance_harvest(bd_handle h, int k, float* xyz4, int* speci
   std::vector<float4> r(len);
   const float4* cur = h->hctrl->cur ? h->state1.p : h->state0.p;
   if (len) BD_CUDA(cudaMemcpy(r.data(), cur + base[k], len * sizeof(float4), cudaMemcpyDeviceToHost));
+  // The step's last phase puts reaction products in their reactants' slots,
+  // so the state is in canonical order only up to those slots; the next
+  // sort (a frozen step) restores it.  Harvest in canonical order, so the
+  // result does not depend on how many frozen steps ran before it.
+  canonical_sort(h->hinst[k], &r);
   size_t m = 0;
   for (const float4& q : r) {
     uint32_t w;
@@ -1325,7 +1381,7 @@ BD_API const char* bd_stage_name(bd_handle h, int k) {
 BD_API bd_status bd_get_kernels_per_step(bd_handle h, int* n) {
   if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
   if (h->diffuse_only()) *n = (h->Z > 0 ? 2 : 0) + 2;
-  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 7 : 8);
+  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 7 : 8) + (h->B > 0 ? 1 : 0);
   return BD_OK;
 }
 
@@ -1422,8 +1478,7 @@ BD_API bd_status bd_get_species_d(bd_handle h, int inst, int species, float* D) 
 
 BD_API bd_status bd_set_launch_shape(bd_handle h, int bs, int cs, int bp, int cp) {
   if (!h) return BD_ERR_INVALID_ARGUMENT;
-  for (int b : {bs, bp})
-    if (b < 32 || b > 256 || b % 32) return BD_ERR_INVALID_ARGUMENT;
+  if (bs < 32 || bs > 256 || bs % 32 || bp != 256) return BD_ERR_INVALID_ARGUMENT;
   if (cs < 1 || cs > 64 || cp < 1 || cp > 64) return BD_ERR_INVALID_ARGUMENT;
   h->shape.block_stream = bs;
   h->shape.grid_stream = h->n_sm * cs;

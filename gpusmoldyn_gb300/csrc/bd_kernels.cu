@@ -55,6 +55,30 @@ __device__ __forceinline__ uint32_t ctrl_status_warp(const DevCtrl* c) {
   return __shfl_sync(kFull, s, 0);
 }
 
+// Grid-stride loop over the records [0, n_total) of the step: body(i, rec)
+// with rec the current record for i < n_real (indices from n_real on are the
+// step's zeroth-order births).  The next iteration's record is loaded before
+// the body runs, so each thread keeps two 16-byte loads in flight.  Every
+// thread of a warp makes the same number of calls (warp collectives allowed).
+template <class Body>
+__device__ __forceinline__ void stream_records(const float4* __restrict__ st, uint32_t n_real, uint32_t n_total,
+                                               Body&& body) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t base = blockIdx.x * blockDim.x;
+  const float4 none = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float4 next = base + threadIdx.x < n_real ? __ldcs(&st[base + threadIdx.x]) : none;
+  for (; base < n_total; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    const float4 rec = next;
+    const uint32_t ahead = i + stride;
+    next = ahead < n_real && ahead > i ? __ldcs(&st[ahead]) : none;
+    // and the record after that towards L2
+    const uint32_t far = ahead + stride;
+    if (far < n_real && far > ahead) asm volatile("prefetch.global.L2 [%0];" ::"l"(st + far));
+    body(i, rec);
+  }
+}
+
 __device__ __forceinline__ const float4* cur_state(const KParams& p, uint32_t cur) {
   return cur ? p.state[1] : p.state[0];
 }
@@ -92,20 +116,48 @@ __device__ __forceinline__ uint32_t word_of(const U4& c, uint32_t k) {
   }
 }
 
+// Instance parameters.  kSingle (a handle with one instance) reads the copy
+// in the kernel parameters, which the compiler folds into constant-bank
+// operands; ensembles read the instance table in global memory.
+template <bool kSingle>
+__device__ __forceinline__ const DevInstance& inst_of(const KParams& p, uint32_t inst) {
+  if (kSingle) return p.inst0;
+  return p.inst[inst];
+}
+
+// What every record of a one-instance handle reads, loaded once per CTA:
+// the instance's flags, step and first slot in registers, its species and
+// first-order tables in shared memory (at most kCtxSpecies / kCtxUni
+// entries; larger networks run the generic kernels).
+constexpr uint32_t kCtxSpecies = 64, kCtxUni = 64;
+struct SingleCtx {
+  uint32_t flags, step, slot_base;
+  const DevSpecies* species;
+  const DevUni* uni;
+};
+
+// Fills the shared tables (all threads of the CTA call it; one barrier).
+__device__ __forceinline__ SingleCtx single_ctx(const KParams& p, DevSpecies* s_species, DevUni* s_uni) {
+  for (uint32_t t = threadIdx.x; t < p.S; t += blockDim.x) s_species[t] = p.species[t];
+  for (uint32_t t = threadIdx.x; t < p.U; t += blockDim.x) s_uni[t] = p.uni[t];
+  __syncthreads();
+  return SingleCtx{ld_u32(&p.inst_flags[0]), ld_u32(&p.inst_step[0]), ld_u32(&p.inst_slot_base[0]), s_species,
+                   s_uni};
+}
+
 // Advance the record in slot i by one step: diffusion, reflection and the
 // first successful first-order reaction (reaction_kernel.cuh:303-341: coins
 // in list order, decay when the first product is absent, a second product
 // becomes a birth).  kCount adds fired reactions to the event counters.
-template <bool kTable, bool kCount>
-__device__ __forceinline__ void advance_real(const KParams& p, const float4* __restrict__ cur, uint32_t i,
-                                             Out2& o) {
+template <bool kTable, bool kCount, bool kSingle>
+__device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& ctx, const float4 rec, uint32_t i,
+                                            Out2& o) {
   o.n = 0;
-  const float4 rec = cur[i];
   const uint32_t w = rec_w(rec);
   if (w == kDead) return;
   const uint32_t inst = w >> 16, sp = w & kSpeciesMask;
-  const DevInstance& I = p.inst[inst];
-  const uint32_t flags = p.inst_flags[inst];
+  const DevInstance& I = inst_of<kSingle>(p, inst);
+  const uint32_t flags = kSingle ? ctx.flags : p.inst_flags[inst];
   if (flags & kInstRemoved) return;
   if ((flags & kInstFrozen) || !(flags & kInstActive)) {
     o.r[0] = rec;
@@ -113,10 +165,10 @@ __device__ __forceinline__ void advance_real(const KParams& p, const float4* __r
     o.n = 1;
     return;
   }
-  const uint32_t local = i - p.inst_slot_base[inst];
-  const uint32_t t = p.inst_step[inst];
+  const uint32_t local = i - (kSingle ? ctx.slot_base : p.inst_slot_base[inst]);
+  const uint32_t t = kSingle ? ctx.step : p.inst_step[inst];
   const uint32_t k0 = I.key_lo, k1 = I.key_hi;
-  const DevSpecies S = p.species[I.block * p.S + sp];
+  const DevSpecies S = kSingle ? ctx.species[sp] : p.species[I.block * p.S + sp];
 
   const U4 rn = philox(U4{local, t, kTagDiffuse, 0u}, k0, k1);
   float g0, g1, g2;
@@ -131,7 +183,7 @@ __device__ __forceinline__ void advance_real(const KParams& p, const float4* __r
   U4 coins = rn;
   for (uint32_t k = 0; k < S.uni_count; ++k) {
     if (k > 0 && ((k - 1) & 3u) == 0) coins = philox(U4{local, t, kTagUniCoin | ((k - 1) >> 2), 0u}, k0, k1);
-    const DevUni& u = p.uni[I.block * p.U + S.uni_begin + k];
+    const DevUni& u = kSingle ? ctx.uni[S.uni_begin + k] : p.uni[I.block * p.U + S.uni_begin + k];
     if (u32_to_unit(k == 0 ? rn.w : word_of(coins, k - 1)) < u.prob) {
       if (kCount) atomicAdd(&p.pending[(size_t)inst * p.R + u.rxn], 1ull);
       if (u.prod0 < 0) return;  // decay: no record
@@ -162,6 +214,7 @@ __device__ __forceinline__ void advance_real(const KParams& p, const float4* __r
 
 // Zeroth-order birth number v of this step: uniform position in the box
 // (reaction_cpu.cpp:44-60 with randPos, particleSystem.h:115-120).
+template <bool kSingle>
 __device__ __forceinline__ void advance_virtual(const KParams& p, uint32_t v, Out2& o) {
   const uint32_t nz = p.n_inst * p.Z;
   // entry e with zero_off[e] <= v < zero_off[e + 1]
@@ -173,7 +226,7 @@ __device__ __forceinline__ void advance_virtual(const KParams& p, uint32_t v, Ou
   }
   const uint32_t inst = lo / p.Z, zr = lo % p.Z;
   const uint32_t k_local = v - p.zero_off[inst * p.Z];
-  const DevInstance& I = p.inst[inst];
+  const DevInstance& I = inst_of<kSingle>(p, inst);
   const uint32_t t = p.inst_step[inst];
   const U4 r = philox(U4{k_local, t, kTagZeroPos, 0u}, I.key_lo, I.key_hi);
   const float x = fminf(__fmaf_rn(u24_to_unit(r.x), __fsub_rn(I.hi[0], I.lo[0]), I.lo[0]), I.hi[0]);
@@ -207,19 +260,6 @@ __device__ __forceinline__ uint32_t warp_claim(uint32_t* cnt, uint32_t key) {
   if (key != kNoKey && lane_id() == (uint32_t)leader) old = atomicSub(&cnt[key], (uint32_t)__popc(peers));
   old = __shfl_sync(kFull, old, leader);
   return old - 1u - rank;
-}
-
-// Binned sort: lanes with equal keys take consecutive places of their
-// cell's bin with one atomic; the count keeps growing past the bin size so
-// an overflow reports the occupancy it needs.
-__device__ __forceinline__ uint32_t warp_claim_add(uint32_t* cnt, uint32_t key) {
-  const uint32_t peers = __match_any_sync(kFull, key);
-  const int leader = __ffs(peers) - 1;
-  const uint32_t rank = __popc(peers & ((1u << lane_id()) - 1u));
-  uint32_t old = 0;
-  if (key != kNoKey && lane_id() == (uint32_t)leader) old = atomicAdd(&cnt[key], (uint32_t)__popc(peers));
-  old = __shfl_sync(kFull, old, leader);
-  return old + rank;
 }
 
 template <int kThreads>
@@ -298,23 +338,25 @@ __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
 
 // kMinBlocks 4 / 6 cap registers at 64 / 40 (50% / 75% occupancy, the
 // latter with a few spills); the launch shape picks the variant.
-template <bool kTable, int kMinBlocks>
+template <bool kTable, int kMinBlocks, bool kSingle>
 __global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
-  const DevCtrl* c = p.ctrl;
+  __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
+  __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
+  SingleCtx ctx{};
+  if (kSingle) ctx = single_ctx(p, s_species, s_uni);
+  DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
   const uint32_t cur = ld_u32(&c->cur);
   const float4* __restrict__ st = cur_state(p, cur);
   const uint32_t n_real = ld_u32(&c->n_slots), n_total = n_real + ld_u32(&c->n_virtual);
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n_total; base += stride) {
-    const uint32_t i = base + threadIdx.x;
+  stream_records(st, n_real, n_total, [&](uint32_t i, const float4& rec) {
     Out2 o;
     o.n = 0;
-    if (i < n_real) advance_real<kTable, true>(p, st, i, o);
-    else if (i < n_total) advance_virtual(p, i - n_real, o);
+    if (i < n_real) advance_rec<kTable, true, kSingle>(p, ctx, rec, i, o);
+    else if (i < n_total) advance_virtual<kSingle>(p, i - n_real, o);
     warp_count(p.cell_count, o.n > 0 ? o.key[0] : kNoKey);
     if (__any_sync(kFull, o.n > 1)) warp_count(p.cell_count, o.n > 1 ? o.key[1] : kNoKey);
-  }
+  });
 }
 
 __global__ void __launch_bounds__(1024) k_scan_tiles(KParams p) {
@@ -373,20 +415,22 @@ __global__ void __launch_bounds__(1024) k_scan_down(KParams p) {
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) p.cell_start[p.n_cells] = ld_u32(&c->n_sorted);
 }
 
-template <bool kTable, int kMinBlocks>
+template <bool kTable, int kMinBlocks, bool kSingle>
 __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
+  __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
+  __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
+  SingleCtx ctx{};
+  if (kSingle) ctx = single_ctx(p, s_species, s_uni);
   DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
   const uint32_t cur = ld_u32(&c->cur);
   const float4* __restrict__ st = cur_state(p, cur);
   const uint32_t n_real = ld_u32(&c->n_slots), n_total = n_real + ld_u32(&c->n_virtual);
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n_total; base += stride) {
-    const uint32_t i = base + threadIdx.x;
+  stream_records(st, n_real, n_total, [&](uint32_t i, const float4& rec) {
     Out2 o;
     o.n = 0;
-    if (i < n_real) advance_real<kTable, false>(p, st, i, o);
-    else if (i < n_total) advance_virtual(p, i - n_real, o);
+    if (i < n_real) advance_rec<kTable, false, kSingle>(p, ctx, rec, i, o);
+    else if (i < n_total) advance_virtual<kSingle>(p, i - n_real, o);
     const int kmax = __any_sync(kFull, o.n > 1) ? 2 : 1;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -399,43 +443,76 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
         else atomicOr(&c->status, kStatBounds);
       }
     }
+  });
+}
+
+// A record waiting for its place in a bin: the warp's claim (atomicAdd on
+// the cell count by the lane that leads the cell's peers) is issued when
+// the record is made and consumed one record later, so the atomic's round
+// trip to L2 overlaps the next record's arithmetic instead of stalling it.
+struct PendingClaim {
+  float4 r;
+  uint32_t key;     // kNoKey: nothing pending in this lane
+  uint32_t old;     // leader lane: count before the warp's claim
+  uint32_t leader;  // lane holding `old` for this lane's cell
+  uint32_t rank;    // this lane's place among its cell's peers
+};
+
+__device__ __forceinline__ PendingClaim claim_issue(uint32_t* cnt, uint32_t key, const float4& r) {
+  PendingClaim c;
+  c.r = r;
+  c.key = key;
+  const uint32_t peers = __match_any_sync(kFull, key);
+  c.leader = (uint32_t)(__ffs(peers) - 1);
+  c.rank = __popc(peers & ((1u << lane_id()) - 1u));
+  c.old = 0;
+  if (key != kNoKey && lane_id() == c.leader) c.old = atomicAdd(&cnt[key], (uint32_t)__popc(peers));
+  return c;
+}
+
+__device__ __forceinline__ void claim_retire(const KParams& p, DevCtrl* c, const PendingClaim& pc) {
+  const uint32_t off = __shfl_sync(kFull, pc.old, pc.leader) + pc.rank;
+  if (pc.key == kNoKey) return;
+  if (off < p.bin_cap) {
+    p.bins[(size_t)pc.key * p.bin_cap + off] = pc.r;
+  } else {
+    atomicOr(&c->status, kStatBins);
+    atomicMax(&c->bin_need, off + 1u);
   }
 }
 
 // Binned path, pass 1 of 2: advance every record (as k_count) and write it
 // into the next free place of its cell's bin.  Replaces k_count + k_scatter:
-// the step's arithmetic runs once and nothing is recomputed.
-template <bool kTable, int kMinBlocks>
+// the step's arithmetic runs once and nothing is recomputed.  First
+// products keep the deferred claim above; the rare second products (births)
+// claim and store at once.
+template <bool kTable, int kMinBlocks, bool kSingle>
 __global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
+  __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
+  __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
+  SingleCtx ctx{};
+  if (kSingle) ctx = single_ctx(p, s_species, s_uni);
   DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
   const uint32_t cur = ld_u32(&c->cur);
   const float4* __restrict__ st = cur_state(p, cur);
   const uint32_t n_real = ld_u32(&c->n_slots), n_total = n_real + ld_u32(&c->n_virtual);
-  const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t K = p.bin_cap;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n_total; base += stride) {
-    const uint32_t i = base + threadIdx.x;
+  PendingClaim pending;
+  pending.key = kNoKey;
+  pending.old = 0;
+  pending.leader = 0;
+  pending.rank = 0;
+  stream_records(st, n_real, n_total, [&](uint32_t i, const float4& rec) {
     Out2 o;
     o.n = 0;
-    if (i < n_real) advance_real<kTable, true>(p, st, i, o);
-    else if (i < n_total) advance_virtual(p, i - n_real, o);
-    const int kmax = __any_sync(kFull, o.n > 1) ? 2 : 1;
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      if (k >= kmax) break;  // warp-uniform
-      const uint32_t key = o.n > k ? o.key[k] : kNoKey;
-      const uint32_t off = warp_claim_add(p.cell_count, key);
-      if (key != kNoKey) {
-        if (off < K) {
-          p.bins[(size_t)key * K + off] = o.r[k];
-        } else {
-          atomicOr(&c->status, kStatBins);
-          atomicMax(&c->bin_need, off + 1u);
-        }
-      }
-    }
-  }
+    if (i < n_real) advance_rec<kTable, true, kSingle>(p, ctx, rec, i, o);
+    else if (i < n_total) advance_virtual<kSingle>(p, i - n_real, o);
+    const PendingClaim next = claim_issue(p.cell_count, o.n > 0 ? o.key[0] : kNoKey, o.r[0]);
+    if (__any_sync(kFull, o.n > 1)) claim_retire(p, c, claim_issue(p.cell_count, o.n > 1 ? o.key[1] : kNoKey, o.r[1]));
+    claim_retire(p, c, pending);
+    pending = next;
+  });
+  claim_retire(p, c, pending);
 }
 
 // Position of record r among the records of its cell [s, e) in canonical
@@ -458,12 +535,11 @@ __device__ __forceinline__ float dist2(const float4& a, const float4& b) {
 // Append candidate pair (lo < hi, canonical slots) of local reaction b,
 // after its coin when the reaction probability is below 1.
 __device__ __forceinline__ void emit_pair(const KParams& p, DevCtrl* c, uint32_t lo, uint32_t hi, int32_t b,
-                                          float prob, uint32_t inst, const DevInstance* __restrict__ Ip,
-                                          uint32_t cbase) {
+                                          float prob, uint32_t inst, const DevInstance& I) {
   if (prob < 1.0f) {
-    const uint32_t base_new = __ldg(&p.cell_start[cbase]);
-    const U4 u = philox(U4{lo - base_new, __ldg(&p.inst_step[inst]), kTagBimCoin, hi - base_new},
-                        __ldg(&Ip->key_lo), __ldg(&Ip->key_hi));
+    const uint32_t base_new = __ldg(&p.cell_start[I.cell_base]);
+    const U4 u = philox(U4{lo - base_new, __ldg(&p.inst_step[inst]), kTagBimCoin, hi - base_new}, I.key_lo,
+                        I.key_hi);
     if (!(u32_to_unit(u.x) < prob)) return;
   }
   const uint32_t idx = atomicAdd(&c->n_pairs, 1u);
@@ -472,9 +548,9 @@ __device__ __forceinline__ void emit_pair(const KParams& p, DevCtrl* c, uint32_t
 }
 
 // Cells with more records than this are handed from k_pairs_cells to
-// k_pairs_big, which gives each of them a whole CTA.
+// k_pairs_big_sort / k_pairs_big_pairs, which give each of them a whole CTA.
 constexpr uint32_t kBigCell = 128;
-constexpr int kBigGrid = 304;  // CTAs of k_pairs_big (cells it takes in turn)
+constexpr int kBigGrid = 304;  // CTAs of the large-cell kernels (cells they take in turn)
 
 // First record of a cell: its bin, or its range of the compact scatter buffer.
 template <bool kBinned>
@@ -487,25 +563,27 @@ struct Seeker {
   float4 r;
   uint32_t inst, block;
   float max_r, r2max;
+  float xlim;          // |dx| bound of every pair within its binding radii
   const int32_t* row;  // second-order table row of its species
-  const DevInstance* Ip;
 };
 
 // False when the record takes no part in this step's pair search: born in
 // this step, instance not advancing, or a species without second-order
 // reactions.
+template <bool kSingle>
 __device__ __forceinline__ bool seeker_init(const KParams& p, const float4& r, Seeker& k) {
   const uint32_t w = rec_w(r);
   if (w & kNewborn) return false;
   k.r = r;
   k.inst = w >> 16;
   if (!advancing(__ldg(&p.inst_flags[k.inst]))) return false;
-  k.Ip = p.inst + k.inst;
-  k.block = __ldg(&k.Ip->block);
+  k.block = inst_of<kSingle>(p, k.inst).block;
   const uint32_t sa = w & kSpeciesMask;
   k.max_r = __ldg(&p.species[k.block * p.S + sa].max_r);
   // a bound on every squared radius of the species (float rounding of max_r^2)
   k.r2max = k.max_r * k.max_r * 1.0001f;
+  // fl(dx^2) <= d2 <= r2max, so |dx| <= max_r * 1.00005
+  k.xlim = k.max_r * 1.001f;
   k.row = p.bim_table + sa * p.S;
   return k.max_r > 0.0f;
 }
@@ -513,6 +591,7 @@ __device__ __forceinline__ bool seeker_init(const KParams& p, const float4& r, S
 // Local second-order reaction of k with record q when q lies within its
 // binding radius, else -1.
 __device__ __forceinline__ int32_t pair_reaction(const KParams& p, const Seeker& k, const float4& q) {
+  if (fabsf(__fsub_rn(q.x, k.r.x)) > k.xlim) return -1;
   const uint32_t wq = rec_w(q);
   if (wq & kNewborn) return -1;
   const float d2 = dist2(k.r, q);
@@ -522,36 +601,44 @@ __device__ __forceinline__ int32_t pair_reaction(const KParams& p, const Seeker&
   return b;
 }
 
+template <bool kSingle>
 __device__ __forceinline__ void emit(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t ca, uint32_t cq,
                                      int32_t b) {
-  emit_pair(p, c, min(ca, cq), max(ca, cq), b, __ldg(&p.bim[k.block * p.B + (uint32_t)b].prob), k.inst, k.Ip,
-            __ldg(&k.Ip->cell_base));
+  emit_pair(p, c, min(ca, cq), max(ca, cq), b, __ldg(&p.bim[k.block * p.B + (uint32_t)b].prob), k.inst,
+            inst_of<kSingle>(p, k.inst));
 }
 
 // Pairs of record k (canonical slot ca, in `cell`) with the records of the
 // 13 forward neighbour cells (higher key) whose shared face, edge or corner
 // lies within its largest binding radius.  Every cross-cell pair within
 // range is found from its lower-key side only, so each is tested once.
-template <bool kBinned>
-__device__ void search_forward(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t cell, uint32_t ca) {
-  const DevInstance* __restrict__ Ip = k.Ip;
-  const uint32_t cbase = __ldg(&Ip->cell_base);
-  const float cl0 = __ldg(&Ip->cell[0]), cl1 = __ldg(&Ip->cell[1]), cl2 = __ldg(&Ip->cell[2]);
-  const uint32_t d0 = __ldg(&Ip->dims[0]), d1 = __ldg(&Ip->dims[1]), d2 = __ldg(&Ip->dims[2]);
-  const uint32_t local = cell - cbase;
-  const int cx = (int)(local % d0), cy = (int)((local / d0) % d1), cz = (int)(local / (d0 * d1));
+// The record's cell coordinates are recomputed from its position exactly
+// as the sort computed its key (cell_coord), which avoids integer division.
+template <bool kBinned, bool kSingle>
+__device__ __forceinline__ void search_forward(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t ca) {
+  const DevInstance& I = inst_of<kSingle>(p, k.inst);
+  const float cl0 = I.cell[0], cl1 = I.cell[1], cl2 = I.cell[2];
+  const uint32_t d0 = I.dims[0], d1 = I.dims[1], d2 = I.dims[2];
+  const float gx = __fmul_rn(__fsub_rn(k.r.x, I.lo[0]), I.inv[0]);
+  const float gy = __fmul_rn(__fsub_rn(k.r.y, I.lo[1]), I.inv[1]);
+  const float gz = __fmul_rn(__fsub_rn(k.r.z, I.lo[2]), I.inv[2]);
+  const int cx = min(max((int)floorf(gx), 0), (int)d0 - 1);
+  const int cy = min(max((int)floorf(gy), 0), (int)d1 - 1);
+  const int cz = min(max((int)floorf(gz), 0), (int)d2 - 1);
   const float margin = p.prune_margin * fminf(cl0, fminf(cl1, cl2));
-  const float fx = __fsub_rn(__fmul_rn(__fsub_rn(k.r.x, __ldg(&Ip->lo[0])), __ldg(&Ip->inv[0])), (float)cx);
-  const float fy = __fsub_rn(__fmul_rn(__fsub_rn(k.r.y, __ldg(&Ip->lo[1])), __ldg(&Ip->inv[1])), (float)cy);
-  const float fz = __fsub_rn(__fmul_rn(__fsub_rn(k.r.z, __ldg(&Ip->lo[2])), __ldg(&Ip->inv[2])), (float)cz);
-  const float lox = fx * cl0, hix = (1.0f - fx) * cl0;
-  const float loy = fy * cl1, hiy = (1.0f - fy) * cl1;
-  const float hiz = (1.0f - fz) * cl2;
-  const float need = k.max_r + margin, need2 = need * need;
+  const float need = k.max_r + margin;
+  const float fx = __fsub_rn(gx, (float)cx), fy = __fsub_rn(gy, (float)cy), fz = __fsub_rn(gz, (float)cz);
+  const float hix = (1.0f - fx) * cl0, hiy = (1.0f - fy) * cl1, hiz = (1.0f - fz) * cl2;
+  // every forward neighbour lies across the +x, +y or +z face
   const int zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
-  const int ylo = (cy > 0 && loy <= need) ? -1 : 0, yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
-  const int xlo = (cx > 0 && lox <= need) ? -1 : 0, xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
+  const int yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
+  const int xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
   if ((zhi | yhi | xhi) == 0) return;
+  const float lox = fx * cl0, loy = fy * cl1;
+  const float need2 = need * need;
+  const int ylo = (cy > 0 && loy <= need) ? -1 : 0;
+  const int xlo = (cx > 0 && lox <= need) ? -1 : 0;
+  const uint32_t cbase = I.cell_base;
   for (int dz = 0; dz <= zhi; ++dz) {
     const float ddz = dz > 0 ? hiz : 0.0f;
     for (int dy = (dz > 0 ? ylo : 0); dy <= yhi; ++dy) {
@@ -561,11 +648,12 @@ __device__ void search_forward(const KParams& p, DevCtrl* c, const Seeker& k, ui
         if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
         const uint32_t nkey = cbase + ((uint32_t)(cz + dz) * d1 + (uint32_t)(cy + dy)) * d0 + (uint32_t)(cx + dx);
         const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
+        if (nn > kBigCell) continue;  // pairs with large cells are found by k_pairs_big_pairs
         const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
         for (uint32_t m = 0; m < nn; ++m) {
           const float4 q = __ldg(&nb[m]);
           const int32_t b = pair_reaction(p, k, q);
-          if (b >= 0) emit(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
+          if (b >= 0) emit<kSingle>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
         }
       }
     }
@@ -575,18 +663,21 @@ __device__ void search_forward(const KParams& p, DevCtrl* c, const Seeker& k, ui
 // Canonical order + pair search, one warp per 32 consecutive cells.  The
 // warp walks the cells' records 32 at a time (lane t of a round = record t
 // of the cells' concatenation), so each lane handles one record whatever
-// the cell sizes.  For its record a lane
-//   * counts the records of the cell that precede it in canonical order and
-//     writes it to cell_start[cell] + that rank in the next state;
-//   * in the same loop, tests the cell's later records (storage order)
-//     against its binding radii, each in-cell pair once;
+// the cell sizes; there are no CTA-wide barriers.  For its record a lane
+//   * counts the records of its cell that precede it in canonical order,
+//     reading only their x words (records whose x bits occur twice in the
+//     cell are ranked again on all four words), and writes it to
+//     cell_start[cell] + that rank in the next state;
+//   * in the same loop marks the cell's later records (storage order)
+//     whose x lies within its largest binding radius; only those are read
+//     in full and tested, each in-cell pair once;
 //   * searches the forward neighbour cells (search_forward).
 // Canonical slots of partners are computed only for pairs within range.
-// Cells above kBigCell records are queued for k_pairs_big.  kBinned: the
+// Cells above kBigCell records are queued for the large-cell kernels.  kBinned: the
 // records come from the cell bins, whose counts are cleared here for the
 // next step; otherwise from the compact scatter buffer.
-template <bool kHasBim, bool kBinned>
-__global__ void __launch_bounds__(256) k_pairs_cells(KParams p) {
+template <bool kHasBim, bool kBinned, bool kSingle>
+__global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   __shared__ uint32_t s_cell[8][32], s_cs[8][32], s_n[8][32], s_off[8][32];
   DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
@@ -596,7 +687,12 @@ __global__ void __launch_bounds__(256) k_pairs_cells(KParams p) {
   const uint32_t n_tasks = (p.n_cells + 31u) >> 5;
   const uint32_t nw = gridDim.x * (blockDim.x >> 5);
   const uint32_t le_mask = lane == 31 ? kFull : ((2u << lane) - 1u);
-  for (uint32_t task = blockIdx.x * (blockDim.x >> 5) + warp; task < n_tasks; task += nw) {
+  // Cells are taken from the highest key down: the bins written last by
+  // k_bin (its records stream in ascending cell order) are still in L2,
+  // and the next state's low slots, written last here, are the first the
+  // next step's k_bin reads.
+  for (uint32_t tk = blockIdx.x * (blockDim.x >> 5) + warp; tk < n_tasks; tk += nw) {
+    const uint32_t task = n_tasks - 1u - tk;
     const uint32_t cell = task * 32u + lane;
     uint32_t cs = 0, n = 0;
     if (cell < p.n_cells) {
@@ -636,13 +732,20 @@ __global__ void __launch_bounds__(256) k_pairs_cells(KParams p) {
         const float4* __restrict__ cb = cell_records<kBinned>(p, ocell, ocs);
         const float4 ra = __ldg(&cb[j]);
         Seeker k;
-        const bool search = kHasBim && seeker_init(p, ra, k);
-        uint32_t rank = 0, cand = 0;  // cand: bit m = later member m < 32 within range
+        const bool search = kHasBim && seeker_init<kSingle>(p, ra, k);
+        const float xlim = search ? k.xlim : -1.0f;
+        const uint32_t rx = __float_as_uint(ra.x);
+        const float* __restrict__ cbx = reinterpret_cast<const float*>(cb);
+        uint32_t rank = 0, cand = 0;  // cand: bit m = later member m < 32 with |dx| within range
+        bool tie = false;
         for (uint32_t m = 0; m < on; ++m) {
-          const float4 qm = __ldg(&cb[m]);
-          rank += (rec_less(qm, ra) || (m < j && rec_equal(qm, ra))) ? 1u : 0u;
-          if (search && m > j && m < 32u && pair_reaction(p, k, qm) >= 0) cand |= 1u << m;
+          const float qx = __ldg(&cbx[4 * m]);
+          const uint32_t qb = __float_as_uint(qx);
+          rank += qb < rx ? 1u : 0u;
+          tie |= qb == rx && m != j;
+          if (m > j && m < 32u && fabsf(__fsub_rn(qx, ra.x)) <= xlim) cand |= 1u << m;
         }
+        if (tie) rank = canonical_rank(cb, 0, on, j, ra);
         const uint32_t ca = ocs + rank;
         if (ca < p.capacity) nx[ca] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
         else atomicOr(&c->status, kStatBounds);
@@ -651,14 +754,15 @@ __global__ void __launch_bounds__(256) k_pairs_cells(KParams p) {
             const uint32_t m = (uint32_t)(__ffs(cand) - 1);
             cand &= cand - 1u;
             const float4 qm = __ldg(&cb[m]);
-            emit(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), pair_reaction(p, k, qm));
+            const int32_t bb = pair_reaction(p, k, qm);
+            if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
           }
           for (uint32_t m = max(j + 1u, 32u); m < on; ++m) {  // cells of 33..kBigCell records
             const float4 qm = __ldg(&cb[m]);
-            const int32_t b = pair_reaction(p, k, qm);
-            if (b >= 0) emit(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), b);
+            const int32_t bb = pair_reaction(p, k, qm);
+            if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
           }
-          search_forward<kBinned>(p, c, k, ocell, ca);
+          search_forward<kBinned, kSingle>(p, c, k, ca);
         }
       }
       before += __popc(M);
@@ -667,48 +771,239 @@ __global__ void __launch_bounds__(256) k_pairs_cells(KParams p) {
   }
 }
 
-// Cells queued by k_pairs_cells (more than kBigCell records, e.g. particles
-// released at one point), one CTA per cell: ranks first (kept in
-// rank_scratch by storage position), then the pairs, which read the
-// partners' ranks instead of recounting them.
-template <bool kHasBim, bool kBinned>
-__global__ void __launch_bounds__(256) k_pairs_big(KParams p) {
+constexpr uint32_t kBigChunk = 2048;  // records sorted per shared-memory pass
+
+// Records in [0, len) of the sorted run `run` that order before `e`
+// (kOrEqual: before or equal).
+template <bool kOrEqual>
+__device__ __forceinline__ uint32_t run_rank(const float4* run, uint32_t len, const float4& e) {
+  uint32_t lo = 0, hi = len;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const float4 q = run[mid];
+    if (rec_less(q, e) || (kOrEqual && rec_equal(q, e))) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// CTA-uniform status read (the large-cell kernels use barriers).
+__device__ __forceinline__ bool stop_block(const DevCtrl* c) {
   __shared__ uint32_t s_stop;
-  DevCtrl* c = p.ctrl;
   if (threadIdx.x == 0) s_stop = ld_u32(&c->status);
   __syncthreads();
-  if (s_stop) return;
+  const bool stop = s_stop != 0;
+  __syncthreads();
+  return stop;
+}
+
+// Large cells, part 1 of 2: the cells queued by k_pairs_cells (more than
+// kBigCell records, e.g. particles released at one point), one CTA per
+// cell, sorted in O(n log^2 n) rather than ranked in O(n^2):
+//   1. chunks of 2048 records are sorted in shared memory (bitonic network,
+//      padded with all-ones records) into big_scratch;
+//   2. merge passes (each record finds its place in the partner run by
+//      binary search) double the sorted runs, alternating between
+//      big_scratch and the next state, until the cell is one canonical run;
+//   3. the run is left in both places: in the next state without newborn
+//      marks, in big_scratch (indexed by canonical slot) with them, where
+//      k_pairs_big_pairs reads it.
+// The first step that queues a cell without big_scratch in place raises
+// kStatScratch; the host allocates it and replays the step.
+template <bool kBinned>
+__global__ void __launch_bounds__(256) k_pairs_big_sort(KParams p) {
+  __shared__ float4 s_rec[kBigChunk];
+  DevCtrl* c = p.ctrl;
+  if (stop_block(c)) return;
+  const uint32_t nbig = min(ld_u32(&c->n_big), p.big_cap);
+  if (nbig == 0) return;
+  if (p.big_scratch_cap < p.capacity) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&c->status, kStatScratch);
+    return;
+  }
   const uint32_t cur = ld_u32(&c->cur);
-  float4* __restrict__ nx = next_state(p, cur);
+  float4* nx = next_state(p, cur);
+  const float4 pad = make_float4(__uint_as_float(kFull), __uint_as_float(kFull), __uint_as_float(kFull),
+                                 __uint_as_float(kFull));
+  for (uint32_t bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
+    const uint32_t cell = p.big[bi];
+    const uint32_t cs = p.cell_start[cell], n = p.cell_start[cell + 1] - cs;
+    if ((uint64_t)cs + n > p.capacity) {
+      if (threadIdx.x == 0) atomicOr(&c->status, kStatBounds);
+      continue;  // uniform over the CTA
+    }
+    const float4* __restrict__ cb = cell_records<kBinned>(p, cell, cs);
+    float4* out = nx + cs;
+    float4* tmp = p.big_scratch + cs;
+    for (uint32_t c0 = 0; c0 < n; c0 += kBigChunk) {
+      const uint32_t len = min(kBigChunk, n - c0);
+      for (uint32_t i = threadIdx.x; i < kBigChunk; i += blockDim.x) s_rec[i] = i < len ? cb[c0 + i] : pad;
+      __syncthreads();
+      for (uint32_t k = 2; k <= kBigChunk; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+          for (uint32_t i = threadIdx.x; i < kBigChunk; i += blockDim.x) {
+            const uint32_t ixj = i ^ j;
+            if (ixj > i) {
+              const float4 a = s_rec[i], b = s_rec[ixj];
+              const bool up = (i & k) == 0;
+              if (rec_less(b, a) == up) {
+                s_rec[i] = b;
+                s_rec[ixj] = a;
+              }
+            }
+          }
+          __syncthreads();
+        }
+      }
+      for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) tmp[c0 + i] = s_rec[i];
+      __syncthreads();
+    }
+    float4* src = tmp;
+    float4* dst = out;
+    for (uint32_t w = kBigChunk; w < n; w <<= 1) {
+      for (uint32_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        const uint32_t lo = idx / (2 * w) * (2 * w);
+        const uint32_t mid = min(lo + w, n), hi = min(lo + 2 * w, n);
+        const float4 e = src[idx];
+        const uint32_t pos = idx < mid ? (idx - lo) + run_rank<false>(src + mid, hi - mid, e)
+                                       : (idx - mid) + run_rank<true>(src + lo, mid - lo, e);
+        dst[lo + pos] = e;
+      }
+      __syncthreads();
+      float4* t = src;
+      src = dst;
+      dst = t;
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const float4 r = src[i];
+      tmp[i] = r;
+      out[i] = make_float4(r.x, r.y, r.z, __uint_as_float(rec_w(r) & ~kNewborn));
+    }
+    __syncthreads();
+  }
+}
+
+// Index of the first record of the sorted run [0, n) whose x has its sign
+// bit set: canonical order sorts x >= 0 ascending, then negative x by |x|.
+__device__ __forceinline__ uint32_t run_negative_start(const float4* run, uint32_t n) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__float_as_uint(run[mid].x) & 0x80000000u) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+// First record of [lo, hi) (sorted by |x| within one sign) with |x| >= v.
+__device__ __forceinline__ uint32_t run_abs_lower(const float4* run, uint32_t lo, uint32_t hi, float v) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (fabsf(run[mid].x) < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Pairs of seeker k (canonical slot ca) with the records of a sorted run
+// (canonical slots base + m) whose |x - k.x| is within k.xlim, skipping
+// m <= skip_to (in-cell: only later records; else pass -1).
+template <bool kSingle>
+__device__ void sweep_sorted(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t ca, const float4* run,
+                             uint32_t n, uint32_t base, int64_t skip_to) {
+  const uint32_t npos = run_negative_start(run, n);
+  // bounds widened well past any rounding of x0 +- xlim; the pair test decides
+  const float x0 = k.r.x, w = 2.0f * k.xlim + 1e-6f * fabsf(x0);
+  const float lo = x0 - w, hi = x0 + w;
+  if (hi >= 0.0f) {  // x >= 0 part, ascending
+    for (uint32_t m = run_abs_lower(run, 0, npos, fmaxf(lo, 0.0f)); m < npos; ++m) {
+      const float4 q = run[m];
+      if (q.x > hi) break;
+      if ((int64_t)m <= skip_to) continue;
+      const int32_t b = pair_reaction(p, k, q);
+      if (b >= 0) emit<kSingle>(p, c, k, ca, base + m, b);
+    }
+  }
+  if (lo <= 0.0f) {  // x < 0 part, ascending |x|
+    for (uint32_t m = run_abs_lower(run, npos, n, fmaxf(-hi, 0.0f)); m < n; ++m) {
+      const float4 q = run[m];
+      if (fabsf(q.x) > -lo) break;
+      if ((int64_t)m <= skip_to) continue;
+      const int32_t b = pair_reaction(p, k, q);
+      if (b >= 0) emit<kSingle>(p, c, k, ca, base + m, b);
+    }
+  }
+}
+
+// Large cells, part 2 of 2, one CTA per queued cell, on the canonical runs
+// left by part 1.  Each pair involving a large cell is tested once:
+//   * inside the cell, by x sweeps over the run;
+//   * with a large neighbour, from the lower-key cell of the two, by x
+//     sweeps over the neighbour's run (binary search to |dx| <= radius);
+//   * with an ordinary neighbour, here, in either direction, by a loop
+//     over its records (k_pairs_cells skips large forward neighbours).
+template <bool kHasBim, bool kBinned>
+__global__ void __launch_bounds__(256) k_pairs_big_pairs(KParams p) {
+  DevCtrl* c = p.ctrl;
+  if (!kHasBim || stop_block(c)) return;
   const uint32_t nbig = min(ld_u32(&c->n_big), p.big_cap);
   for (uint32_t bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
     const uint32_t cell = p.big[bi];
     const uint32_t cs = p.cell_start[cell], n = p.cell_start[cell + 1] - cs;
-    const float4* __restrict__ cb = cell_records<kBinned>(p, cell, cs);
-    for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
-      const float4 ra = cb[t];
-      const uint32_t rank = canonical_rank(cb, 0, n, t, ra);
-      if (cs + t < p.capacity && cs + rank < p.capacity) {
-        p.rank_scratch[cs + t] = rank;
-        nx[cs + rank] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
-      } else {
-        atomicOr(&c->status, kStatBounds);
+    if ((uint64_t)cs + n > p.capacity) continue;
+    const float4* run = p.big_scratch + cs;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      Seeker k;
+      if (!seeker_init<false>(p, run[i], k)) continue;
+      const uint32_t ca = cs + i;
+      sweep_sorted<false>(p, c, k, ca, run, n, cs, (int64_t)i);
+      const DevInstance& I = p.inst[k.inst];
+      const float cl0 = I.cell[0], cl1 = I.cell[1], cl2 = I.cell[2];
+      const uint32_t d0 = I.dims[0], d1 = I.dims[1], d2 = I.dims[2];
+      const float gx = __fmul_rn(__fsub_rn(k.r.x, I.lo[0]), I.inv[0]);
+      const float gy = __fmul_rn(__fsub_rn(k.r.y, I.lo[1]), I.inv[1]);
+      const float gz = __fmul_rn(__fsub_rn(k.r.z, I.lo[2]), I.inv[2]);
+      const int cx = min(max((int)floorf(gx), 0), (int)d0 - 1);
+      const int cy = min(max((int)floorf(gy), 0), (int)d1 - 1);
+      const int cz = min(max((int)floorf(gz), 0), (int)d2 - 1);
+      const float margin = p.prune_margin * fminf(cl0, fminf(cl1, cl2));
+      const float need = k.max_r + margin, need2 = need * need;
+      const float fx = __fsub_rn(gx, (float)cx), fy = __fsub_rn(gy, (float)cy), fz = __fsub_rn(gz, (float)cz);
+      const float dlo[3] = {fx * cl0, fy * cl1, fz * cl2};
+      const float dhi[3] = {(1.0f - fx) * cl0, (1.0f - fy) * cl1, (1.0f - fz) * cl2};
+      const int c3[3] = {cx, cy, cz};
+      const int dm[3] = {(int)d0, (int)d1, (int)d2};
+      int lo3[3], hi3[3];
+      for (int a = 0; a < 3; ++a) {
+        lo3[a] = (c3[a] > 0 && dlo[a] <= need) ? -1 : 0;
+        hi3[a] = (c3[a] + 1 < dm[a] && dhi[a] <= need) ? 1 : 0;
       }
-    }
-    __syncthreads();
-    if (kHasBim) {
-      for (uint32_t t = threadIdx.x; t < n && cs + n <= p.capacity; t += blockDim.x) {
-        Seeker k;
-        if (!seeker_init(p, cb[t], k)) continue;
-        const uint32_t ca = cs + p.rank_scratch[cs + t];
-        for (uint32_t m = t + 1; m < n; ++m) {
-          const int32_t b = pair_reaction(p, k, cb[m]);
-          if (b >= 0) emit(p, c, k, ca, cs + p.rank_scratch[cs + m], b);
+      for (int dz = lo3[2]; dz <= hi3[2]; ++dz) {
+        const float ddz = dz < 0 ? dlo[2] : (dz > 0 ? dhi[2] : 0.0f);
+        for (int dy = lo3[1]; dy <= hi3[1]; ++dy) {
+          const float ddy = dy < 0 ? dlo[1] : (dy > 0 ? dhi[1] : 0.0f);
+          for (int dx = lo3[0]; dx <= hi3[0]; ++dx) {
+            if (dx == 0 && dy == 0 && dz == 0) continue;
+            const float ddx = dx < 0 ? dlo[0] : (dx > 0 ? dhi[0] : 0.0f);
+            if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
+            const bool forward = dz > 0 || (dz == 0 && (dy > 0 || (dy == 0 && dx > 0)));
+            const uint32_t nkey =
+                I.cell_base + ((uint32_t)(cz + dz) * d1 + (uint32_t)(cy + dy)) * d0 + (uint32_t)(cx + dx);
+            const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
+            if (nn > kBigCell) {
+              if (forward) sweep_sorted<false>(p, c, k, ca, p.big_scratch + ns, nn, ns, -1);
+              continue;  // a large lower-key neighbour finds this pair itself
+            }
+            const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
+            for (uint32_t m = 0; m < nn; ++m) {
+              const float4 q = __ldg(&nb[m]);
+              const int32_t b = pair_reaction(p, k, q);
+              if (b >= 0) emit<false>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
+            }
+          }
         }
-        search_forward<kBinned>(p, c, k, cell, ca);
       }
     }
-    __syncthreads();
   }
 }
 
@@ -855,7 +1150,7 @@ __global__ void __launch_bounds__(256) k_diffuse(KParams p) {
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     Out2 o;
-    advance_real<kTable, false>(p, st, i, o);
+    advance_rec<kTable, false, false>(p, SingleCtx{}, st[i], i, o);
     if (o.n > 0) st[i] = o.r[0];
   }
 }
@@ -869,7 +1164,7 @@ __global__ void __launch_bounds__(256) k_append(KParams p) {
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += stride) {
     Out2 o;
-    advance_virtual(p, v, o);
+    advance_virtual<false>(p, v, o);
     st[n + v] = make_float4(o.r[0].x, o.r[0].y, o.r[0].z, __uint_as_float(rec_w(o.r[0]) & ~kNewborn));
   }
 }
@@ -956,22 +1251,35 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   }
   // Register-capped variants of the streaming kernels, picked by the launch
   // shape's resident CTAs per SM: 1 = no cap, 4 = 64 registers, 6 = 40.
-#define BD_STREAM_LAUNCH(KERNEL)                                   \
-  do {                                                             \
-    switch (shape.min_blocks) {                                    \
-      case 6:                                                      \
-        if (table) KERNEL<true, 6><<<gs, bs, 0, s>>>(p);           \
-        else KERNEL<false, 6><<<gs, bs, 0, s>>>(p);                \
-        break;                                                     \
-      case 4:                                                      \
-        if (table) KERNEL<true, 4><<<gs, bs, 0, s>>>(p);           \
-        else KERNEL<false, 4><<<gs, bs, 0, s>>>(p);                \
-        break;                                                     \
-      default:                                                     \
-        if (table) KERNEL<true, 1><<<gs, bs, 0, s>>>(p);           \
-        else KERNEL<false, 1><<<gs, bs, 0, s>>>(p);                \
-    }                                                              \
+#define BD_STREAM_LAUNCH3(KERNEL, MINB)                                                    \
+  do {                                                                                     \
+    if (single) {                                                                          \
+      if (table) KERNEL<true, MINB, true><<<gs, bs, 0, s>>>(p);                             \
+      else KERNEL<false, MINB, true><<<gs, bs, 0, s>>>(p);                                  \
+    } else {                                                                               \
+      if (table) KERNEL<true, MINB, false><<<gs, bs, 0, s>>>(p);                            \
+      else KERNEL<false, MINB, false><<<gs, bs, 0, s>>>(p);                                 \
+    }                                                                                      \
   } while (0)
+#define BD_STREAM_LAUNCH(KERNEL)                   \
+  do {                                             \
+    switch (shape.min_blocks) {                    \
+      case 6: BD_STREAM_LAUNCH3(KERNEL, 6); break; \
+      case 4: BD_STREAM_LAUNCH3(KERNEL, 4); break; \
+      default: BD_STREAM_LAUNCH3(KERNEL, 1);       \
+    }                                              \
+  } while (0)
+#define BD_PAIRS_LAUNCH(BINNED)                                                                      \
+  do {                                                                                               \
+    if (single) {                                                                                    \
+      if (has_bim) k_pairs_cells<true, BINNED, true><<<shape.grid_pairs, 256, 0, s>>>(p);       \
+      else k_pairs_cells<false, BINNED, true><<<shape.grid_pairs, 256, 0, s>>>(p);              \
+    } else {                                                                                         \
+      if (has_bim) k_pairs_cells<true, BINNED, false><<<shape.grid_pairs, 256, 0, s>>>(p);      \
+      else k_pairs_cells<false, BINNED, false><<<shape.grid_pairs, 256, 0, s>>>(p);             \
+    }                                                                                                \
+  } while (0)
+  const bool single = p.n_inst == 1 && p.S <= kCtxSpecies && p.U <= kCtxUni;
   if (path == Path::kBinned) {
     BD_STREAM_LAUNCH(k_bin);
     done("k_bin");
@@ -981,12 +1289,14 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     done("k_scan_top");
     k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
     done("k_scan_down");
-    if (has_bim) k_pairs_cells<true, true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
-    else k_pairs_cells<false, true><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+    BD_PAIRS_LAUNCH(true);
     done("k_pairs_cells");
-    if (has_bim) k_pairs_big<true, true><<<kBigGrid, 256, 0, s>>>(p);
-    else k_pairs_big<false, true><<<kBigGrid, 256, 0, s>>>(p);
-    done("k_pairs_big");
+    k_pairs_big_sort<true><<<kBigGrid, 256, 0, s>>>(p);
+    done("k_pairs_big_sort");
+    if (has_bim) {
+      k_pairs_big_pairs<true, true><<<kBigGrid, 256, 0, s>>>(p);
+      done("k_pairs_big_pairs");
+    }
     k_match<<<1, 1024, 0, s>>>(p);
     done("k_match");
     return n;
@@ -1000,14 +1310,18 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
   done("k_scan_down");
   BD_STREAM_LAUNCH(k_scatter);
-#undef BD_STREAM_LAUNCH
   done("k_scatter");
-  if (has_bim) k_pairs_cells<true, false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
-  else k_pairs_cells<false, false><<<shape.grid_pairs, shape.block_pairs, 0, s>>>(p);
+  BD_PAIRS_LAUNCH(false);
+#undef BD_STREAM_LAUNCH
+#undef BD_STREAM_LAUNCH3
+#undef BD_PAIRS_LAUNCH
   done("k_pairs_cells");
-  if (has_bim) k_pairs_big<true, false><<<kBigGrid, 256, 0, s>>>(p);
-  else k_pairs_big<false, false><<<kBigGrid, 256, 0, s>>>(p);
-  done("k_pairs_big");
+  k_pairs_big_sort<false><<<kBigGrid, 256, 0, s>>>(p);
+  done("k_pairs_big_sort");
+  if (has_bim) {
+    k_pairs_big_pairs<true, false><<<kBigGrid, 256, 0, s>>>(p);
+    done("k_pairs_big_pairs");
+  }
   k_match<<<1, 1024, 0, s>>>(p);
   done("k_match");
   return n;

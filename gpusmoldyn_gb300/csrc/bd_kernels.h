@@ -14,6 +14,7 @@ struct KParams {
   float4* bins;               // [n_cells][bin_cap] records per cell (binned sort)
   DevCtrl* ctrl;
   const DevInstance* inst;
+  DevInstance inst0;          // copy of instance 0 (kernels specialised for one instance)
   const DevSpecies* species;  // [block][S]
   const DevUni* uni;          // [block][U]
   const DevBim* bim;          // [block][B]
@@ -38,8 +39,8 @@ struct KParams {
   uint32_t capacity, pair_cap;
   uint32_t bin_cap;           // records per cell bin (binned sort)
   uint32_t* big;              // [big_cap] cells queued for k_pairs_big
-  uint32_t* rank_scratch;     // [capacity] canonical ranks inside queued cells
-  uint32_t big_cap;
+  float4* big_scratch;        // [big_scratch_cap] merge-sort buffer of k_pairs_big
+  uint32_t big_cap, big_scratch_cap;
   float prune_margin;         // fraction of a cell edge added to pruning distances
 };
 

@@ -117,6 +117,7 @@ enum StatusBits : uint32_t {
   kStatBounds = 4u,        // a device-side bounds check failed
   kStatTimeout = 8u,       // a bounded wait ran out
   kStatBins = 16u,         // a cell held more records than its bin
+  kStatScratch = 32u,      // the large-cell kernel needs its sort buffer
 };
 
 // Pair list entry written by the pair kernel and resolved by the matcher.

@@ -251,7 +251,8 @@ BD_API bd_status bd_get_species_d(bd_handle h, int instance, int species, float 
 BD_API bd_status bd_set_cell_size(bd_handle h, float cell_size);
 /* Launch shape of the particle kernels (autotuner): threads per CTA (a
  * multiple of 32, at most 256) and CTAs per SM of the grid-stride grids, for
- * the streaming kernels and for the pair kernel.  A streaming grid of
+ * the streaming kernels and for the pair kernel (whose CTA is always 256
+ * threads, one per cell of a tile: block_pairs must be 256).  A streaming grid of
  * exactly 48 or 32 warps per SM runs register-capped kernel variants (40 or
  * 64 registers) so that all of it is resident.  The result of a step does
  * not depend on it. */
@@ -300,9 +301,10 @@ BD_API bd_status bd_get_instance_reaction_info(bd_handle h, int instance, int rx
  * added and finalized as usual; then bd_instance_admit adds a simulation,
  * bd_step advances every admitted instance together, an instance freezes on
  * the device when it reaches its step count, bd_instance_poll lists frozen
- * instances and bd_instance_harvest copies one out and frees its slot.  An
- * instance evolves exactly as it would alone.  The reference runs one
- * system per process and has no counterpart. */
+ * instances and bd_instance_harvest copies one out (in canonical order: by
+ * cell, then by record bits) and frees its slot.  An instance evolves
+ * exactly as it would alone.  The reference runs one system per process and
+ * has no counterpart. */
 BD_API bd_status bd_create_server(const bd_config *cfg, int max_instances, bd_handle *out);
 BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc *d, const float *xyz4, const int *species,
                                    size_t n, uint32_t steps, int *slot);

@@ -272,3 +272,56 @@ def test_bin_overflow_grows_and_replays_exactly():
     compact.synchronize()
     np.testing.assert_array_equal(gpu_records(binned), gpu_records(compact))
     assert np.diff(binned.cells()).max() > 100
+
+
+@pytest.mark.parametrize("sort", SORTS)
+def test_large_system_bit_exact(sort):
+    """1.2M particles, species in contiguous blocks of the initial array: the
+    streaming kernels' grid-stride loops wrap several times per thread and
+    the pair kernel takes several cell tasks per warp, so a record read from
+    the wrong chunk or a cell handled twice changes species counts and
+    positions and shows here."""
+    side = 31.0
+    s = System((0, 0, 0), (side,) * 3, dt=1e-3, seed=26, normals="table", sort=sort)
+    A, B, Cc = s.add_species(1.0), s.add_species(1.0), s.add_species(0.5)
+    s.add_reaction(2, [A, B], [Cc], 0.05)
+    s.add_reaction(1, [Cc], [], 5.0)
+    s.finalize()
+    n = 1_200_000
+    g = rng(26)
+    pos = uniform_positions(g, n, (0, 0, 0), (side,) * 3)
+    sp = np.repeat(np.arange(3, dtype=np.int32), [n // 2, n // 2 - n // 10, n // 10])
+    s.set_particles(pos, sp)
+    _, npairs, ev = run_parity(s, 3)
+    assert npairs > 100 and ev[0] > 100
+
+
+@pytest.mark.parametrize("sort", SORTS)
+def test_clusters_across_cell_corners_bit_exact(sort):
+    """Dense clusters around a cell corner make eight neighbouring cells
+    large (more than 128 records: sorted by the large-cell kernels), next to
+    ordinary cells: pairs inside large cells, between two large cells and
+    between a large and an ordinary cell must all match the oracle."""
+    side, n, n_cl = 2.0, 6000, 1600
+
+    def make(pos, sp):
+        s = System((0, 0, 0), (side,) * 3, dt=1e-3, seed=27, normals="table", sort=sort)
+        A, B, Cc = s.add_species(0.2), s.add_species(0.2), s.add_species(0.1)
+        s.add_reaction(2, [A, B], [Cc], 0.5)
+        s.finalize()
+        s.set_particles(pos, sp)
+        return s
+    g = rng(27)
+    pos = uniform_positions(g, n, (0, 0, 0), (side,) * 3)
+    sp = (np.arange(n) % 2).astype(np.int32)
+    probe = make(pos, sp)
+    dims, cell, _ = probe.grid()
+    probe.close()
+    corner = np.array([6, 6, 6], np.float32) * cell.astype(np.float32)
+    pos[:n_cl] = uniform_positions(g, n_cl, corner - 0.04, corner + 0.04)
+    c3 = np.clip(np.floor(pos / cell.astype(np.float32)).astype(np.int64), 0, dims.astype(np.int64) - 1)
+    occupancy = np.bincount((c3[:, 2] * dims[1] + c3[:, 1]) * dims[0] + c3[:, 0])
+    assert np.sum(occupancy > 128) >= 4  # large cells at the start
+    s = make(pos, sp)
+    _, npairs, ev = run_parity(s, 5)
+    assert npairs > 0 and ev[0] > 0
