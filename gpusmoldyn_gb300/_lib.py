@@ -27,6 +27,9 @@ BD_ERR_CUDA = 21
 BD_ERR_TIMEOUT = 22
 BD_ERR_NO_DEVICE = 23
 BD_ERR_DEVICE_STATE = 24
+BD_ERR_UNSUPPORTED = 25
+
+BD_DEVICE_NONE = -1
 
 BD_NORMALS_BOXMULLER = 0
 BD_NORMALS_TABLE = 1
@@ -62,6 +65,11 @@ class bd_instance_desc(C.Structure):
     _fields_ = [("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("seed", C.c_uint64),
                 ("d_scale", C.c_float), ("k2_scale", C.c_float), ("cell_size", C.c_float),
                 ("reserved", C.c_uint32 * 3)]
+
+
+class bd_model_info(C.Structure):
+    _fields_ = [("time_start", C.c_double), ("time_stop", C.c_double), ("steps", C.c_uint64),
+                ("n_molecules", C.c_uint64), ("n_species", C.c_int), ("n_reactions", C.c_int)]
 
 
 H = C.c_void_p
@@ -114,6 +122,16 @@ _SIGS = {
     "bd_instance_state": (C.c_int, [H, C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "bd_cell_sort_static": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.POINTER(C.c_uint32), P, P, P]),
+    "bd_get_config": (C.c_int, [H, C.POINTER(bd_config)]),
+    "bd_write_snapshot": (C.c_int, [H, C.c_char_p, C.c_int]),
+    "bd_set_species_name": (C.c_int, [H, C.c_int, C.c_char_p]),
+    "bd_find_species": (C.c_int, [H, C.c_char_p, C.POINTER(C.c_int)]),
+    "bd_set_reaction_name": (C.c_int, [H, C.c_int, C.c_char_p]),
+    "bd_find_reaction": (C.c_int, [H, C.c_char_p, C.POINTER(C.c_int)]),
+    "bd_create_from_model": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(H), C.POINTER(bd_model_info), C.c_char_p,
+                                       C.c_size_t]),
+    "bd_create_from_model_file": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(H), C.POINTER(bd_model_info),
+                                            C.c_char_p, C.c_size_t]),
     "bd_numrxnrate": (C.c_double, [C.c_double, C.c_double, C.c_double]),
     "bd_actrxnrate": (C.c_double, [C.c_double, C.c_double]),
     "bd_bindingradius": (C.c_double, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),

@@ -68,6 +68,7 @@ struct bd_system {
   std::vector<bd_instance_desc> idesc;
   std::vector<float> D;
   std::vector<ReactionDef> rx;
+  std::vector<std::string> species_names, reaction_names;  // optional, "" when unnamed
   bool finalized = false;
   std::vector<DerivedParams> derived;  // one per instance (= parameter block)
 
@@ -1498,6 +1499,47 @@ BD_API bd_status bd_set_cell_size(bd_handle h, float cell_size) {
   if (!h || !(cell_size >= 0)) return BD_ERR_INVALID_ARGUMENT;
   h->cell_override = cell_size;
   return BD_OK;
+}
+
+namespace {
+bd_status set_name(std::vector<std::string>* names, size_t n, int id, const char* name) {
+  if (!name || id < 0 || (size_t)id >= n) return BD_ERR_INVALID_ARGUMENT;
+  names->resize(n);
+  (*names)[id] = name;
+  return BD_OK;
+}
+bd_status find_name(const std::vector<std::string>& names, const char* name, int* id) {
+  if (!name || !id) return BD_ERR_INVALID_ARGUMENT;
+  for (size_t k = 0; k < names.size(); k++)
+    if (names[k] == name) {
+      *id = (int)k;
+      return BD_OK;
+    }
+  return BD_ERR_INVALID_ARGUMENT;
+}
+}  // namespace
+
+BD_API bd_status bd_get_config(bd_handle h, bd_config* out) {
+  if (!h || !out) return BD_ERR_INVALID_ARGUMENT;
+  *out = h->cfg;
+  return BD_OK;
+}
+
+BD_API bd_status bd_set_species_name(bd_handle h, int species, const char* name) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  return set_name(&h->species_names, h->D.size(), species, name);
+}
+BD_API bd_status bd_find_species(bd_handle h, const char* name, int* species) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  return find_name(h->species_names, name, species);
+}
+BD_API bd_status bd_set_reaction_name(bd_handle h, int rxn, const char* name) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  return set_name(&h->reaction_names, h->rx.size(), rxn, name);
+}
+BD_API bd_status bd_find_reaction(bd_handle h, const char* name, int* rxn) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  return find_name(h->reaction_names, name, rxn);
 }
 
 BD_API double bd_numrxnrate(double step, double a, double b) { return numrxnrate(step, a, b); }

@@ -71,6 +71,46 @@ class System:
         self.n_species = 0
         self.n_reactions = 0
 
+    @classmethod
+    def from_model(cls, text=None, path=None, device=0):
+        """A finalized system with its molecules placed, from a model in the
+        Smoldyn-style configuration language (bd_create_from_model).  Returns
+        (system, info) with info the time span and counts the model declared."""
+        self = cls.__new__(cls)
+        self.lib = L.load()
+        self.server = False
+        self.h = C.c_void_p()
+        info = L.bd_model_info()
+        err = C.create_string_buffer(512)
+        dev = L.BD_DEVICE_NONE if device is None else device
+        if path is not None:
+            rc = self.lib.bd_create_from_model_file(str(path).encode(), dev, C.byref(self.h), C.byref(info), err, 512)
+        else:
+            rc = self.lib.bd_create_from_model(text.encode(), dev, C.byref(self.h), C.byref(info), err, 512)
+        if rc != L.BD_OK:
+            raise L.BDError(rc, f"model: {err.value.decode()}")
+        cfg = L.bd_config()
+        L.check(self.lib.bd_get_config(self.h, C.byref(cfg)), "bd_get_config")
+        self.cfg = cfg
+        self.dt = cfg.dt
+        self.n_instances = 1
+        self.instances = [dict(box_lo=tuple(cfg.box_lo), box_hi=tuple(cfg.box_hi), seed=cfg.seed, d_scale=1.0,
+                               k2_scale=1.0, cell_size=0.0)]
+        self.n_species = info.n_species
+        self.n_reactions = info.n_reactions
+        return self, dict(time_start=info.time_start, time_stop=info.time_stop, steps=info.steps,
+                          n_molecules=info.n_molecules)
+
+    def species_id(self, name: str) -> int:
+        i = C.c_int()
+        L.check(self.lib.bd_find_species(self.h, name.encode(), C.byref(i)), f"species {name}")
+        return i.value
+
+    def reaction_id(self, name: str) -> int:
+        i = C.c_int()
+        L.check(self.lib.bd_find_reaction(self.h, name.encode(), C.byref(i)), f"reaction {name}")
+        return i.value
+
     # ------------------------------------------------------------- set-up
     def add_species(self, D: float) -> int:
         i = C.c_int()
@@ -282,6 +322,10 @@ class System:
         k = C.c_int()
         L.check(self.lib.bd_get_kernels_per_step(self.h, C.byref(k)), "kernels_per_step")
         return k.value
+
+    def write_snapshot(self, path, binary=False):
+        """Write the molecules to `path` (bd_write_snapshot)."""
+        L.check(self.lib.bd_write_snapshot(self.h, str(path).encode(), 1 if binary else 0), "write_snapshot")
 
     def state_pointer(self):
         p = C.c_void_p()

@@ -333,6 +333,50 @@ BD_API bd_status bd_instance_state(bd_handle h, int slot, uint32_t *steps, uint3
 BD_API bd_status bd_cell_sort_static(const float *d_in, uint64_t n, const float box_lo[3], const float box_hi[3],
                                      const uint32_t dims[3], float *d_out, uint32_t *d_cell_start, void *stream);
 
+/* ----------------------------------------------------------- snapshots */
+/* The molecules written to a file (no display: replaces the reference's
+ * OpenGL viewer, render_particles.cpp / particles.cpp).  TEXT: "# step s
+ * molecules n species S", "# counts c0 c1 ...", then "x y z species" per
+ * molecule with 9 significant digits (exact for float).  BINARY: uint64
+ * step, uint64 n, then n records of float x, y, z and int32 species. */
+enum { BD_SNAPSHOT_TEXT = 0, BD_SNAPSHOT_BINARY = 1 };
+BD_API bd_status bd_write_snapshot(bd_handle h, const char *path, int format);
+
+/* The configuration a handle was created with (box, dt, seed, ...). */
+BD_API bd_status bd_get_config(bd_handle h, bd_config *out);
+
+/* ------------------------------------------------------------- names */
+/* Optional names of species and reactions (the model reader sets them). */
+BD_API bd_status bd_set_species_name(bd_handle h, int species, const char *name);
+BD_API bd_status bd_find_species(bd_handle h, const char *name, int *species);
+BD_API bd_status bd_set_reaction_name(bd_handle h, int rxn, const char *name);
+BD_API bd_status bd_find_reaction(bd_handle h, const char *name, int *rxn);
+
+/* ------------------------------------------------------- model reader */
+/* What a model text declared besides the network (all zero when absent). */
+typedef struct bd_model_info {
+  double time_start, time_stop;
+  uint64_t steps;             /* (time_stop - time_start) / time_step, rounded */
+  uint64_t n_molecules;       /* placed by mol statements */
+  int n_species, n_reactions;
+} bd_model_info;
+
+/* A finalized handle with its molecules placed, from a model in a subset of
+ * Smoldyn's configuration language: dim 3, boundaries / low_wall /
+ * high_wall (reflecting), species, difc, time_start / time_stop /
+ * time_step, random_seed, reaction, reaction_rate, reaction_probability,
+ * product_placement (irrev, pgem, pgemmax, unbindrad), mol (coordinates or
+ * u for uniform, from a splitmix64 stream seeded by random_seed),
+ * end_file; display and output statements are ignored.  Replaces the
+ * reference's hard-coded presets ParticleSystem::test1Reactions ..
+ * test3Types (particleSystem.cpp:319-571), whose comments quote these
+ * statements.  device may be BD_DEVICE_NONE.  On failure err (if given)
+ * receives "line N: reason". */
+BD_API bd_status bd_create_from_model(const char *text, int device, bd_handle *out, bd_model_info *info, char *err,
+                                      size_t err_cap);
+BD_API bd_status bd_create_from_model_file(const char *path, int device, bd_handle *out, bd_model_info *info,
+                                           char *err, size_t err_cap);
+
 /* ------------------------------------------------------ rxnparam (host) */
 /* Restatements of rxnparam.h:39-42 (Andrews-Bray rate tables, rxnparam.cpp:
  * 42-308): rate per step in length^3, binding radius, unbinding radius. */
