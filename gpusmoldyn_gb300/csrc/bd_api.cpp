@@ -836,6 +836,30 @@ BD_API bd_status bd_step(bd_handle h, int nsteps) {
   return BD_OK;
 }
 
+BD_API bd_status bd_step_async(bd_handle h, int nsteps, void* stream) {
+  if (!h || nsteps < 0) return BD_ERR_INVALID_ARGUMENT;
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  BD_CUDA(cudaSetDevice(h->device));
+  cudaStream_t caller = (cudaStream_t)stream;
+  cudaEvent_t before, after;
+  BD_CUDA(cudaEventCreateWithFlags(&before, cudaEventDisableTiming));
+  if (!cuda_ok(cudaEventCreateWithFlags(&after, cudaEventDisableTiming), "cudaEventCreate")) {
+    cudaEventDestroy(before);
+    return BD_ERR_CUDA;
+  }
+  bd_status st = BD_OK;
+  if (!cuda_ok(cudaEventRecord(before, caller), "cudaEventRecord") ||
+      !cuda_ok(cudaStreamWaitEvent(h->stream, before, 0), "cudaStreamWaitEvent"))
+    st = BD_ERR_CUDA;
+  if (!st) st = bd_step(h, nsteps);
+  if (!st && (!cuda_ok(cudaEventRecord(after, h->stream), "cudaEventRecord") ||
+              !cuda_ok(cudaStreamWaitEvent(caller, after, 0), "cudaStreamWaitEvent")))
+    st = BD_ERR_CUDA;
+  cudaEventDestroy(before);
+  cudaEventDestroy(after);
+  return st;
+}
+
 BD_API bd_status bd_synchronize(bd_handle h) {
   if (!h) return BD_ERR_INVALID_ARGUMENT;
   if (!h->have_particles) return BD_OK;

@@ -181,8 +181,13 @@ class System:
         L.check(self.lib.bd_set_ensemble_particles(self.h, _ptr(p4), _ptr(sp), _ptr(cnt), len(cnt)),
                 "bd_set_ensemble_particles")
 
-    def step(self, n=1):
-        L.check(self.lib.bd_step(self.h, int(n)), "bd_step")
+    def step(self, n=1, stream=None):
+        """Enqueue n steps; with `stream` (a cudaStream_t as an int) they are
+        ordered after that stream's work and before its later work."""
+        if stream is None:
+            L.check(self.lib.bd_step(self.h, int(n)), "bd_step")
+        else:
+            L.check(self.lib.bd_step_async(self.h, int(n), C.c_void_p(stream)), "bd_step_async")
 
     def synchronize(self, allow_empty=True):
         st = self.lib.bd_synchronize(self.h)

@@ -194,6 +194,13 @@ BD_API bd_status bd_get_state_pointer(bd_handle h, void **dev_records, uint64_t 
  * compactPosAndType (particleSystemCuda.cu:148-367) and zeroReact
  * (reaction_cpu.cpp:36-63). */
 BD_API bd_status bd_step(bd_handle h, int nsteps);
+/* bd_step ordered on a caller's stream (a cudaStream_t; NULL = legacy
+ * default): the steps start after the work already enqueued on `stream`,
+ * and work enqueued on `stream` afterwards starts after the steps.  For a
+ * caller that produces or consumes the device records
+ * (bd_get_state_pointer) on its own stream.  A step that must grow a buffer
+ * and be replayed completes only at the next bd_synchronize. */
+BD_API bd_status bd_step_async(bd_handle h, int nsteps, void *stream);
 
 /* Wait for enqueued steps; if a step ran out of particle or pair capacity
  * the buffers grow and the remaining steps are replayed, so the state after

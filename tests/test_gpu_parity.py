@@ -325,3 +325,18 @@ def test_clusters_across_cell_corners_bit_exact(sort):
     s = make(pos, sp)
     _, npairs, ev = run_parity(s, 5)
     assert npairs > 0 and ev[0] > 0
+
+
+def test_steps_ordered_on_a_caller_stream():
+    """bd_step_async on another stream gives the same trajectory as bd_step."""
+    torch = pytest.importorskip("torch")
+    a = dense_a_b(1500, 1500, 1.5, seed=28, kon=5.0)
+    b = dense_a_b(1500, 1500, 1.5, seed=28, kon=5.0)
+    st = torch.cuda.Stream()
+    for _ in range(3):
+        a.step(4)
+        b.step(4, stream=st.cuda_stream)
+    st.synchronize()
+    a.synchronize()
+    b.synchronize()
+    np.testing.assert_array_equal(gpu_records(a), gpu_records(b))
