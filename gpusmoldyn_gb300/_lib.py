@@ -34,6 +34,9 @@ BD_DEVICE_NONE = -1
 BD_NORMALS_BOXMULLER = 0
 BD_NORMALS_TABLE = 1
 
+BD_PAIR_LAST = 0
+BD_PAIR_CHANNELS = 1
+
 BD_SORT_AUTO = 0
 BD_SORT_COMPACT = 1
 BD_SORT_BINNED = 2
@@ -51,14 +54,15 @@ class bd_config(C.Structure):
     _fields_ = [("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("dt", C.c_float),
                 ("seed", C.c_uint64), ("capacity", C.c_uint64), ("cell_size", C.c_float),
                 ("cell_occupancy", C.c_float), ("normal_mode", C.c_int), ("device", C.c_int),
-                ("pair_capacity", C.c_uint32), ("sort_mode", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+                ("pair_capacity", C.c_uint32), ("sort_mode", C.c_uint32), ("pair_mode", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
 
 
 class bd_reaction_info(C.Structure):
     _fields_ = [("order", C.c_int), ("nprod", C.c_int), ("reactants", C.c_int * 2), ("products", C.c_int * 2),
                 ("rate", C.c_float), ("prob", C.c_float), ("bind_radius", C.c_float),
                 ("unbind_radius", C.c_float), ("geminate_prob", C.c_float), ("product_offsets", C.c_float * 2),
-                ("reverse", C.c_int), ("flags", C.c_int)]
+                ("reverse", C.c_int), ("flags", C.c_int), ("channel_threshold", C.c_float)]
 
 
 class bd_instance_desc(C.Structure):

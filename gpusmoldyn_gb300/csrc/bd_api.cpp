@@ -251,6 +251,7 @@ bd_status validate_config(const bd_config* c) {
   if (!(c->dt > 0)) return BD_ERR_INVALID_ARGUMENT;
   if (c->normal_mode != BD_NORMALS_BOXMULLER && c->normal_mode != BD_NORMALS_TABLE) return BD_ERR_INVALID_ARGUMENT;
   if (c->sort_mode > BD_SORT_BINNED) return BD_ERR_INVALID_ARGUMENT;
+  if (c->pair_mode > BD_PAIR_CHANNELS) return BD_ERR_INVALID_ARGUMENT;
   return BD_OK;
 }
 
@@ -674,6 +675,11 @@ bd_status pack_blocks(bd_system* h) {
       db.off0 = P.rx[r].off[0];
       db.off1 = P.rx[r].off[1];
       db.rxn = (uint32_t)r;
+      db.thresh = P.rx[r].thresh;
+      db.next = -1;
+      if (P.rx[r].next >= 0)
+        for (int b2 = 0; b2 < B; b2++)
+          if (h->bim_list[b2] == P.rx[r].next) db.next = b2;
     }
     for (int z = 0; z < Z; z++) {
       const int r = h->zero_list[z];
@@ -722,14 +728,17 @@ BD_API bd_status bd_finalize(bd_handle h) {
   for (int k = 0; k < I; k++) {
     const bd_instance_desc& d = h->idesc[k];
     const float vol = (d.box_hi[0] - d.box_lo[0]) * (d.box_hi[1] - d.box_lo[1]) * (d.box_hi[2] - d.box_lo[2]);
-    h->derived.push_back(derive_params(h->D, h->rx, h->cfg.dt, vol, d.d_scale, d.k2_scale));
+    h->derived.push_back(derive_params(h->D, h->rx, h->cfg.dt, vol, d.d_scale, d.k2_scale,
+                                       h->cfg.pair_mode == BD_PAIR_CHANNELS));
     if (!first && h->derived.back().status) {
       first = h->derived.back().status;
       g_last_error = h->derived.back().message;
     }
   }
   // fatal setup errors leave the handle unfinalized
-  if (first == BD_ERR_NEGATIVE_RATE || first == BD_ERR_ZERO_DIFFUSION || first == BD_ERR_ILLEGAL_UNBIND) return first;
+  if (first == BD_ERR_NEGATIVE_RATE || first == BD_ERR_ZERO_DIFFUSION || first == BD_ERR_ILLEGAL_UNBIND ||
+      first == BD_ERR_UNSUPPORTED)
+    return first;
 
   // network shape
   h->uni_list.clear();
@@ -751,14 +760,25 @@ BD_API bd_status bd_finalize(bd_handle h) {
   h->Z = (int)h->zero_list.size();
   const int S = h->S, U = h->U, B = h->B, Z = h->Z;
 
-  // pair table: the last reaction listed for a pair wins (particleSystem.cpp:656-669);
-  // a reaction with zero binding radius never fires
+  // pair table: the last reaction listed for a pair wins (particleSystem.cpp:656-669),
+  // or, with competing reactions, the first of the pair's chain; a reaction
+  // with zero rate never fires
   h->bim_table.assign((size_t)S * S, -1);
+  const bool channels = h->cfg.pair_mode == BD_PAIR_CHANNELS;
   for (int b = 0; b < B; b++) {
     const ReactionDef& r = h->rx[h->bim_list[b]];
-    const int v = r.rate > 0 ? b : -1;
-    h->bim_table[(size_t)r.reactants[0] * S + r.reactants[1]] = v;
-    h->bim_table[(size_t)r.reactants[1] * S + r.reactants[0]] = v;
+    if (!(r.rate > 0)) {
+      if (!channels) {
+        h->bim_table[(size_t)r.reactants[0] * S + r.reactants[1]] = -1;
+        h->bim_table[(size_t)r.reactants[1] * S + r.reactants[0]] = -1;
+      }
+      continue;
+    }
+    int32_t& e0 = h->bim_table[(size_t)r.reactants[0] * S + r.reactants[1]];
+    int32_t& e1 = h->bim_table[(size_t)r.reactants[1] * S + r.reactants[0]];
+    if (channels && e0 >= 0) continue;  // the chain starts at the pair's first reaction
+    e0 = b;
+    e1 = b;
   }
 
   bd_status st = pack_blocks(h);
@@ -795,6 +815,7 @@ BD_API bd_status bd_get_instance_reaction_info(bd_handle h, int inst, int rxn, b
   out->geminate_prob = d.gem_prob;
   out->reverse = d.reverse;
   out->flags = d.flags;
+  out->channel_threshold = d.thresh;
   return BD_OK;
 }
 
@@ -1121,7 +1142,8 @@ BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc* d, const
   if (!(dd.d_scale > 0)) dd.d_scale = 1.0f;
   if (!(dd.k2_scale > 0)) dd.k2_scale = 1.0f;
   const float vol = (dd.box_hi[0] - dd.box_lo[0]) * (dd.box_hi[1] - dd.box_lo[1]) * (dd.box_hi[2] - dd.box_lo[2]);
-  DerivedParams P = derive_params(h->D, h->rx, h->cfg.dt, vol, dd.d_scale, dd.k2_scale);
+  DerivedParams P = derive_params(h->D, h->rx, h->cfg.dt, vol, dd.d_scale, dd.k2_scale,
+                                  h->cfg.pair_mode == BD_PAIR_CHANNELS);
   if (P.status == BD_ERR_NEGATIVE_RATE || P.status == BD_ERR_ZERO_DIFFUSION || P.status == BD_ERR_ILLEGAL_UNBIND)
     return P.status;
   std::vector<float4> recs(n);

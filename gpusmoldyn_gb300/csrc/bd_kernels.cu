@@ -1076,9 +1076,19 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
   for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
     const DevPair q = pr[k];
     if (q.state != 1) continue;
-    const uint32_t inst = q.b >> 16, b = q.b & 0xFFFFu;
+    const uint32_t inst = q.b >> 16;
     const DevInstance& I = p.inst[inst];
-    const DevBim br = p.bim[I.block * p.B + b];
+    DevBim br = p.bim[I.block * p.B + (q.b & 0xFFFFu)];
+    if (br.next >= 0) {
+      // competing reactions of this pair: the one whose share of the
+      // pair's summed rate holds the coin
+      const uint32_t base_new = p.cell_start[I.cell_base];
+      const U4 u = philox(U4{q.i - base_new, p.inst_step[inst], kTagBimChannel, q.j - base_new}, I.key_lo,
+                          I.key_hi);
+      const float coin = u24_to_unit(u.x);
+      for (uint32_t hop = 0; hop < p.B && !(coin < br.thresh) && br.next >= 0; ++hop)
+        br = p.bim[I.block * p.B + (uint32_t)br.next];
+    }
     const float4 ri = nx[q.i], rj = nx[q.j];
     const bool i_first = (int32_t)(rec_w(ri) & kSpeciesMask) == br.react0;
     const uint32_t m1 = i_first ? q.i : q.j, m2 = i_first ? q.j : q.i;

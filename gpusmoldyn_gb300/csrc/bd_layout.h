@@ -40,6 +40,7 @@ enum StreamTag : uint32_t {
   kTagZeroPos = 5u << 24,   // position of one zeroth-order birth
   kTagBimCoin = 6u << 24,   // coin of one candidate pair
   kTagBimDir = 7u << 24,    // product direction of one accepted pair
+  kTagBimChannel = 8u << 24,// which competing reaction an accepted pair fires
 };
 
 struct DevSpecies {        // 16 B
@@ -65,7 +66,8 @@ struct DevBim {            // 48 B
   int32_t prod0, prod1;    // product species, -1 = none
   float off0, off1;        // product displacements along a random unit vector
   uint32_t rxn;            // global reaction index
-  uint32_t pad[2];
+  float thresh;            // competing reactions: cumulative share of the pair's rate
+  int32_t next;            // next competing reaction of the pair (local index), -1 = last
 };
 
 struct DevZero {           // 32 B

@@ -245,7 +245,7 @@ void set_status(DerivedParams* P, int code, const std::string& msg) {
 }  // namespace
 
 DerivedParams derive_params(const std::vector<float>& D0, const std::vector<ReactionDef>& rx, float dt,
-                            float volume, float d_scale, float k2_scale) {
+                            float volume, float d_scale, float k2_scale, bool channels) {
   DerivedParams P;
   const int S = (int)D0.size(), R = (int)rx.size();
   P.D.resize(S);
@@ -259,6 +259,38 @@ DerivedParams derive_params(const std::vector<float>& D0, const std::vector<Reac
   P.cdf.assign(R, std::vector<double>());
   P.cdf_kmin.assign(R, 0);
   for (int r = 0; r < R; r++) P.rx[r].reverse = find_reverse(rx, r);
+  // channel mode: reactant pairs with several second-order reactions
+  std::vector<std::vector<int>> groups;
+  std::vector<int> group_of(R, -1);
+  if (channels) {
+    for (int r = 0; r < R; r++) {
+      if (rx[r].order != 2 || !(rx[r].rate > 0)) continue;
+      const int a = std::min(rx[r].reactants[0], rx[r].reactants[1]);
+      const int b = std::max(rx[r].reactants[0], rx[r].reactants[1]);
+      int g = -1;
+      for (size_t k = 0; k < groups.size() && g < 0; k++) {
+        const ReactionDef& f = rx[groups[k][0]];
+        if (std::min(f.reactants[0], f.reactants[1]) == a && std::max(f.reactants[0], f.reactants[1]) == b)
+          g = (int)k;
+      }
+      if (g < 0) {
+        g = (int)groups.size();
+        groups.emplace_back();
+      }
+      groups[g].push_back(r);
+      group_of[r] = g;
+    }
+    for (const std::vector<int>& m : groups) {
+      if (m.size() < 2) continue;
+      // competing reactions are calibrated as irreversible (b = 0): the
+      // reversible coupling of one reaction to its reverse is per pair
+      for (int r : m) {
+        const int u = P.rx[r].reverse;
+        if (u >= 0) P.rx[u].reverse = -1;
+        P.rx[r].reverse = -1;
+      }
+    }
+  }
 
   // order 0: Poisson mean k dt V (smolreact.cpp:295-303)
   for (int r = 0; r < R; r++) {
@@ -310,6 +342,26 @@ DerivedParams derive_params(const std::vector<float>& D0, const std::vector<Reac
       continue;
     }
     float rate3 = rx[r].rate * k2_scale;
+    const int g = group_of[r];
+    if (g >= 0 && groups[g].size() > 1) {
+      // one radius for the pair from the summed rate; each reaction's share
+      // of it picks the reaction of an accepted pair
+      float total = 0.0f, upto = 0.0f;
+      for (int m : groups[g]) total += rx[m].rate;
+      for (size_t k = 0; k < groups[g].size(); k++) {
+        const int m = groups[g][k];
+        upto += rx[m].rate;
+        if (m == r) {
+          d.thresh = k + 1 == groups[g].size() ? 1.0f : upto / total;
+          d.next = k + 1 < groups[g].size() ? groups[g][k + 1] : -1;
+        }
+      }
+      if (rx[r].user_prob >= 0.0f) {
+        set_status(&P, BD_ERR_UNSUPPORTED, "a reaction probability on competing reactions of one pair");
+        continue;
+      }
+      rate3 = total * k2_scale;
+    }
     if (i1 == i2) rate3 *= 2;
     const float dsum = P.D[i1] + P.D[i2];
     const float D1 = P.D[i1], D2 = P.D[i2];

@@ -37,6 +37,11 @@ struct DerivedReaction {
   float x = 0.5f, omx = 0.5f; // order 2 reaction point weights
   int reverse = -1;
   int flags = 0;              // bit 0: pgem fell back to b = 0
+  // competing second-order reactions of one reactant pair (channel mode):
+  // cumulative share of the pair's total rate up to this reaction, and the
+  // next reaction of the pair (-1: last)
+  float thresh = 1.0f;
+  int next = -1;
 };
 
 struct DerivedParams {
@@ -52,8 +57,11 @@ struct DerivedParams {
 // Derive every reaction's parameters for one parameter block.  d_scale and
 // k2_scale multiply the diffusion coefficients and the second-order rates
 // (ensemble instances); volume is the box volume (zeroth order).
+// channels: second-order reactions that share a reactant pair compete (one
+// binding radius from their summed rate, the reaction picked by its share of
+// it); otherwise the last listed reaction of a pair is the pair's reaction.
 DerivedParams derive_params(const std::vector<float>& D, const std::vector<ReactionDef>& rx, float dt,
-                            float volume, float d_scale, float k2_scale);
+                            float volume, float d_scale, float k2_scale, bool channels = false);
 
 // Poisson CDF over [kmin, kmin + len) covering all but ~1e-30 of the mass.
 void poisson_cdf(double mean, std::vector<double>* cdf, int* kmin);

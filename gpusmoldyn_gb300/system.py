@@ -18,11 +18,13 @@ class System:
     ``instances`` (list of dicts with box_lo, box_hi, seed, d_scale, k2_scale,
     cell_size) makes an ensemble of independent instances sharing the
     species and reaction network.  ``sort`` picks how records reach their
-    cells ("auto", "compact" or "binned"; identical results)."""
+    cells ("auto", "compact" or "binned"; identical results); ``pairs``
+    whether several second-order reactions of one reactant pair compete
+    ("channels") or the last listed one is the pair's reaction ("last")."""
 
     def __init__(self, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), dt=1e-3, seed=1, normals="boxmuller",
                  capacity=0, cell_size=0.0, cell_occupancy=0.0, pair_capacity=0, device=0, instances=None,
-                 sort="auto"):
+                 sort="auto", pairs="last"):
         self.lib = L.load()
         self.server = False
         cfg = L.bd_config()
@@ -39,6 +41,7 @@ class System:
         cfg.device = device
         cfg.normal_mode = L.BD_NORMALS_TABLE if normals == "table" else L.BD_NORMALS_BOXMULLER
         cfg.sort_mode = {"auto": L.BD_SORT_AUTO, "compact": L.BD_SORT_COMPACT, "binned": L.BD_SORT_BINNED}[sort]
+        cfg.pair_mode = {"last": L.BD_PAIR_LAST, "channels": L.BD_PAIR_CHANNELS}[pairs]
         self.cfg = cfg
         self.dt = dt
         self.h = C.c_void_p()
@@ -143,7 +146,7 @@ class System:
         return dict(order=ri.order, nprod=ri.nprod, reactants=list(ri.reactants), products=list(ri.products),
                     rate=ri.rate, prob=ri.prob, bind_radius=ri.bind_radius, unbind_radius=ri.unbind_radius,
                     geminate_prob=ri.geminate_prob, product_offsets=list(ri.product_offsets),
-                    reverse=ri.reverse, flags=ri.flags)
+                    reverse=ri.reverse, flags=ri.flags, channel_threshold=ri.channel_threshold)
 
     def species_d(self, instance=0) -> np.ndarray:
         out = np.zeros(self.n_species, np.float32)

@@ -86,6 +86,16 @@ enum {
  * 32 GiB. */
 enum { BD_SORT_AUTO = 0, BD_SORT_COMPACT = 1, BD_SORT_BINNED = 2 };
 
+/* bd_config.pair_mode.  LAST: the last second-order reaction listed for a
+ * reactant pair is the pair's only reaction, as in the reference
+ * (particleSystem.cpp:656-669).  CHANNELS: all of them compete: the pair's
+ * binding radius comes from their summed rate (irreversible calibration,
+ * b = 0) and an accepted pair fires reaction i with probability
+ * rate_i / sum (bd_reaction_info.channel_threshold holds the cumulative
+ * shares).  A reaction probability on a competing reaction is
+ * BD_ERR_UNSUPPORTED. */
+enum { BD_PAIR_LAST = 0, BD_PAIR_CHANNELS = 1 };
+
 typedef struct bd_config {
   float box_lo[3];           /* reflecting box, replaces the fixed [-1,1]^3 world */
   float box_hi[3];           /* (particleSystem.cpp:73, particleSystem.h:114-120) */
@@ -98,7 +108,8 @@ typedef struct bd_config {
   int device;                /* CUDA device ordinal */
   uint32_t pair_capacity;    /* candidate-pair list length; 0 = automatic */
   uint32_t sort_mode;        /* BD_SORT_*: how records reach their cells */
-  uint32_t reserved[6];
+  uint32_t pair_mode;        /* BD_PAIR_*: several second-order reactions of one pair */
+  uint32_t reserved[5];
 } bd_config;
 
 /* Derived parameters of one reaction, as the reference stores them in its
@@ -115,6 +126,7 @@ typedef struct bd_reaction_info {
                                  random unit vector (rxnsetproduct x offsets) */
   int reverse;                /* index of the reverse reaction, -1 if none */
   int flags;                  /* bit 0: pgem fell back to b = 0 */
+  float channel_threshold;    /* BD_PAIR_CHANNELS: cumulative share of the pair's rate (1 = last) */
 } bd_reaction_info;
 
 /* ----------------------------------------------------- lifetime & set-up */

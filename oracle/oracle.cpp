@@ -39,7 +39,7 @@ namespace {
 
 const uint32_t DEAD = 0xFFFFFFFFu;
 const uint32_t T_DIFF = 1u << 24, T_UNI = 2u << 24, T_UNIDIR = 3u << 24, T_ZCOUNT = 4u << 24, T_ZPOS = 5u << 24,
-               T_BIM = 6u << 24, T_BIMDIR = 7u << 24;
+               T_BIM = 6u << 24, T_BIMDIR = 7u << 24, T_BIMCHAN = 8u << 24;
 
 struct Rec {
   float x, y, z;
@@ -134,6 +134,7 @@ struct Model {
   std::vector<float> sigma;
   std::vector<std::vector<int>> uni;  // per species, reaction ids in index order
   std::vector<int> table;             // S*S -> reaction id or -1
+  std::vector<int> next;              // competing reactions: next reaction of the pair, -1 = last
   std::vector<float> r2;              // per reaction
   std::vector<int> zero;              // order-0 reaction ids in index order
   float max_r = 0.0f;
@@ -148,14 +149,27 @@ void build_model(const or_system* s, Model* m) {
   m->uni.assign(S, std::vector<int>());
   m->table.assign((size_t)S * S, -1);
   m->r2.assign(R, 0.0f);
+  m->next.assign(R, -1);
   for (int r = 0; r < R; r++) {
     if (s->order[r] == 1) m->uni[s->react0[r]].push_back(r);
     if (s->order[r] == 0) m->zero.push_back(r);
     if (s->order[r] == 2) {
       m->r2[r] = s->bind_radius[r] * s->bind_radius[r];
-      const int v = m->r2[r] > 0.0f ? r : -1;
-      m->table[(size_t)s->react0[r] * S + s->react1[r]] = v;
-      m->table[(size_t)s->react1[r] * S + s->react0[r]] = v;
+      int& e0 = m->table[(size_t)s->react0[r] * S + s->react1[r]];
+      int& e1 = m->table[(size_t)s->react1[r] * S + s->react0[r]];
+      if (!s->channels) {
+        // the last reaction listed for a pair is the pair's reaction
+        e0 = e1 = m->r2[r] > 0.0f ? r : -1;
+      } else if (m->r2[r] > 0.0f) {
+        // competing reactions: the pair's first reaction starts the chain
+        if (e0 < 0) {
+          e0 = e1 = r;
+        } else {
+          int last = e0;
+          while (m->next[last] >= 0) last = m->next[last];
+          m->next[last] = r;
+        }
+      }
     }
   }
   for (int r = 0; r < R; r++)
@@ -402,7 +416,14 @@ extern "C" int or_step(const or_system* s, uint32_t t, const uint32_t* in, uint3
     for (size_t k = 0; k < cand.size(); k++) {
       if (!acc[k]) continue;
       const Cand& q = cand[k];
-      const int r = q.r;
+      int r = q.r;
+      if (s->channels && m.next[r] >= 0) {
+        // which competing reaction: the one whose share holds the coin
+        uint32_t o[4];
+        m.rng.block(q.i, t, T_BIMCHAN, q.j, o);
+        const float coin = unit24(o[0]);
+        while (!(coin < s->thresh[r]) && m.next[r] >= 0) r = m.next[r];
+      }
       const Rec ri = res[q.i], rj = res[q.j];
       const bool i_first = (int)(ri.w & 0x7FFFu) == s->react0[r];
       const uint32_t m1 = i_first ? q.i : q.j, m2 = i_first ? q.j : q.i;

@@ -36,6 +36,8 @@ typedef struct or_system {
   int sorted;               /* 1: cell-sorted pipeline, 0: in-place diffusion */
   uint32_t inst;            /* instance id written into w */
   int threads;              /* OpenMP threads, 0 = default */
+  int channels;             /* 1: second-order reactions of one pair compete */
+  const float *thresh;      /* per reaction: cumulative share of its pair's rate */
 } or_system;
 
 /* One step.  in/out hold n records of 4 words (x, y, z as float bits, w).

@@ -26,7 +26,7 @@ class or_system(C.Structure):
                 ("R", C.c_int), ("order", ip), ("react0", ip), ("react1", ip), ("prod0", ip), ("prod1", ip),
                 ("prob", fp), ("bind_radius", fp), ("off0", fp), ("off1", fp), ("cdf", dp), ("cdf_off", ip),
                 ("cdf_len", ip), ("cdf_kmin", ip), ("sorted", C.c_int), ("inst", C.c_uint32),
-                ("threads", C.c_int)]
+                ("threads", C.c_int), ("channels", C.c_int), ("thresh", fp)]
 
 
 _lib = None
@@ -76,6 +76,7 @@ class OracleSystem:
         brad = np.array([i["bind_radius"] for i in info] or [0], np.float32)
         off0 = np.array([i["product_offsets"][0] for i in info] or [0], np.float32)
         off1 = np.array([i["product_offsets"][1] for i in info] or [0], np.float32)
+        thresh = np.array([i["channel_threshold"] for i in info] or [1], np.float32)
         cdfs, coff, clen, ckmin = [], [], [], []
         pos = 0
         for r in range(R):
@@ -91,7 +92,7 @@ class OracleSystem:
         cdf_all = np.concatenate(cdfs) if pos else np.zeros(1)
         gauss = gauss_table()
         arrs = dict(order=order, react0=react0, react1=react1, prod0=prod0, prod1=prod1, prob=prob,
-                    bind_radius=brad, off0=off0, off1=off1, D=D.astype(np.float32), gauss=gauss,
+                    bind_radius=brad, off0=off0, off1=off1, thresh=thresh, D=D.astype(np.float32), gauss=gauss,
                     cdf=cdf_all.astype(np.float64), cdf_off=np.array(coff or [0], np.int32),
                     cdf_len=np.array(clen or [0], np.int32), cdf_kmin=np.array(ckmin or [0], np.int32))
         self.arrs = arrs
@@ -111,7 +112,7 @@ class OracleSystem:
         s.R = R
         for name in ("order", "react0", "react1", "prod0", "prod1", "cdf_off", "cdf_len", "cdf_kmin"):
             setattr(s, name, arrs[name].ctypes.data_as(ip))
-        for name in ("prob", "bind_radius", "off0", "off1", "D", "gauss"):
+        for name in ("prob", "bind_radius", "off0", "off1", "thresh", "D", "gauss"):
             setattr(s, name, arrs[name].ctypes.data_as(fp))
         s.cdf = arrs["cdf"].ctypes.data_as(dp)
         if sorted_path is None:
@@ -120,6 +121,7 @@ class OracleSystem:
         s.sorted = 1 if sorted_path else 0
         s.inst = instance
         s.threads = threads
+        s.channels = 1 if getattr(sys.cfg, "pair_mode", 0) == 1 else 0
         self.s = s
         self.n_cells = int(dims[0]) * int(dims[1]) * int(dims[2])
         self.R = R

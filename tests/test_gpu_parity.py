@@ -340,3 +340,23 @@ def test_steps_ordered_on_a_caller_stream():
     a.synchronize()
     b.synchronize()
     np.testing.assert_array_equal(gpu_records(a), gpu_records(b))
+
+
+@pytest.mark.parametrize("sort", SORTS)
+def test_competing_reactions_bit_exact(sort):
+    """Three reactions of one pair compete (pair_mode CHANNELS): the chosen
+    reaction of every accepted pair, its products and the event counters
+    equal the oracle's."""
+    s = System((0, 0, 0), (1.5, 1.5, 1.5), dt=1e-3, seed=29, normals="table", sort=sort, pairs="channels")
+    A, B, Cc, D = (s.add_species(d) for d in (1.0, 1.0, 0.5, 0.3))
+    s.add_reaction(2, [A, B], [Cc], 1.0)
+    s.add_reaction(2, [B, A], [D], 0.5)
+    r = s.add_reaction(2, [A, B], [Cc, D], 2.0)
+    s.set_product_placement(r, L.BD_PP_UNBINDRAD, 0.02)
+    s.add_reaction(2, [Cc, D], [A], 0.5)
+    s.finalize()
+    g = rng(29)
+    pos = uniform_positions(g, 6000, (0, 0, 0), (1.5, 1.5, 1.5))
+    s.set_particles(pos, (np.arange(6000) % 2).astype(np.int32))
+    _, npairs, ev = run_parity(s, 15)
+    assert ev[0] > 30 and ev[1] > 10 and ev[2] > 60

@@ -181,3 +181,32 @@ def test_zeroth_order_production_is_poisson():
     assert counts.var() == pytest.approx(lam, rel=0.2)
     pos, _ = s.particles()
     assert np.all(pos >= 0) and np.all(pos <= side)
+
+
+def test_competing_reactions_split_the_rate():
+    """B + A -> B (k0) and B + A -> B + C (k1) compete for the same pairs
+    (immobile catalysts B): A decays at the rate of the summed k0 + k1, as
+    numrxnrate predicts for the shared binding radius, and the reactions
+    fire in the ratio k0 : k1 (binomial error ~0.3%; tolerance 2%)."""
+    side, rho, dt, k0, k1, steps = 50.0, 10.0, 5e-4, 0.0125, 0.0375, 2000
+    n = int(rho * side ** 3)
+    s = System((0, 0, 0), (side,) * 3, dt=dt, seed=30, pairs="channels")
+    A, B, Cc = s.add_species(2.0), s.add_species(0.0), s.add_species(2.0)
+    s.add_reaction(2, [B, A], [B], k0)
+    s.add_reaction(2, [B, A], [B, Cc], k1)
+    s.finalize()
+    a = s.reaction_info(0)["bind_radius"]
+    g = rng(30)
+    s.set_particles(uniform_positions(g, 2 * n, (0, 0, 0), (side,) * 3),
+                    np.concatenate([np.zeros(n), np.ones(n)]).astype(np.int32))
+    s.step(steps)
+    s.synchronize()
+    na, nb, nc = s.species_counts()
+    e0, e1 = (int(v) for v in s.event_counts()[:2])
+    assert nb == n and e0 + e1 == n - na and nc == e1 and e0 + e1 > 300_000
+    assert e1 / (e0 + e1) == pytest.approx(k1 / (k0 + k1), rel=0.02)
+    T, Dsum, k = steps * dt, 2.0, k0 + k1
+    kstep = numrxnrate(math.sqrt(2 * Dsum * dt), a, -1)
+    k_theory = kstep / dt * (1 + 2 * (k / (4 * math.pi * Dsum)) / math.sqrt(math.pi * Dsum * T))
+    k_meas = -math.log(na / n) / (T * n / side ** 3)
+    assert k_meas / k_theory == pytest.approx(1.0, abs=0.01), (k_meas, k_theory)
