@@ -47,6 +47,23 @@ BD_PP_PGEMMAX = 2
 BD_PP_UNBINDRAD = 3
 BD_PP_OFFSET0 = 4
 
+BD_PANEL_RECT = 0
+BD_PANEL_TRI = 1
+BD_PANEL_SPH = 2
+BD_PANEL_CYL = 3
+BD_PANEL_HEMI = 4
+BD_PANEL_DISK = 5
+
+BD_FACE_FRONT = 0
+BD_FACE_BACK = 1
+BD_FACE_BOTH = 2
+
+BD_SURF_TRANSMIT = 0
+BD_SURF_REFLECT = 1
+BD_SURF_ABSORB = 2
+
+BD_ALL_SPECIES = -1
+
 DEAD = 0xFFFFFFFF
 
 
@@ -74,6 +91,16 @@ class bd_instance_desc(C.Structure):
 class bd_model_info(C.Structure):
     _fields_ = [("time_start", C.c_double), ("time_stop", C.c_double), ("steps", C.c_uint64),
                 ("n_molecules", C.c_uint64), ("n_species", C.c_int), ("n_reactions", C.c_int)]
+
+
+class bd_panel(C.Structure):
+    _fields_ = [("shape", C.c_int), ("axis", C.c_int), ("front", C.c_int), ("p", C.c_float * 10)]
+
+
+class bd_panel_info(C.Structure):
+    _fields_ = [("shape", C.c_int), ("surface", C.c_int), ("axis", C.c_int), ("front", C.c_float),
+                ("a", C.c_float * 3), ("r", C.c_float), ("r2", C.c_float), ("n", C.c_float * 3),
+                ("len", C.c_float), ("v1", C.c_float * 3), ("v2", C.c_float * 3), ("bounds", C.c_float * 4)]
 
 
 H = C.c_void_p
@@ -128,6 +155,12 @@ _SIGS = {
     "bd_cell_sort_static": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.POINTER(C.c_uint32), P, P, P]),
     "bd_get_config": (C.c_int, [H, C.POINTER(bd_config)]),
+    "bd_add_surface": (C.c_int, [H, C.POINTER(C.c_int)]),
+    "bd_set_surface_action": (C.c_int, [H, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "bd_get_surface_action": (C.c_int, [H, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "bd_add_panel": (C.c_int, [H, C.c_int, C.POINTER(bd_panel), C.POINTER(C.c_int)]),
+    "bd_get_panel": (C.c_int, [H, C.c_int, C.POINTER(bd_panel_info)]),
+    "bd_get_surface_counts": (C.c_int, [H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "bd_write_snapshot": (C.c_int, [H, C.c_char_p, C.c_int]),
     "bd_set_species_name": (C.c_int, [H, C.c_int, C.c_char_p]),
     "bd_find_species": (C.c_int, [H, C.c_char_p, C.POINTER(C.c_int)]),

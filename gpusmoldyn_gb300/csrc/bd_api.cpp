@@ -22,6 +22,7 @@
 #include "bd_kernels.h"
 #include "bd_layout.h"
 #include "bd_params.h"
+#include "bd_surface.h"
 
 using namespace bd;
 
@@ -80,6 +81,20 @@ struct bd_system {
   std::vector<int32_t> bim_table;
   bool zero_two_products = false;
 
+  // surfaces: per surface the action of every species not set one by one
+  // (BD_ALL_SPECIES) and the per-species settings (-1 = that default), for
+  // the front and the back face
+  struct Surface {
+    uint8_t all[2] = {kActTransmit, kActTransmit};
+    std::vector<int16_t> species[2];
+  };
+  std::vector<Surface> surfaces;
+  std::vector<bd_panel_info> panels;
+  DevBuf<DevPanel> dpanels;
+  DevBuf<uint8_t> dsurf_act;
+  DevBuf<uint32_t> dpbox_start, dpbox_list;
+  PanelGrid pgrid{};
+
   // device
   int device = 0, n_sm = 152;
   cudaStream_t stream = nullptr;
@@ -125,7 +140,7 @@ struct bd_system {
   DevBuf<uint32_t> inst_flags, inst_target;
 
   bool diffuse_only() const {
-    return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products && !server;
+    return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products && !server && panels.empty();
   }
   Path path() const { return diffuse_only() ? Path::kDiffuseOnly : (binned ? Path::kBinned : Path::kSorted); }
   int n_inst() const { return (int)idesc.size(); }
@@ -183,6 +198,18 @@ KParams make_params(bd_system* h) {
   p.capacity = (uint32_t)h->capacity;
   p.pair_cap = h->pair_cap;
   p.prune_margin = 1e-3f;
+  p.n_panels = (uint32_t)h->panels.size();
+  if (p.n_panels) {
+    p.panels = h->dpanels.p;
+    p.surf_act = h->dsurf_act.p;
+    p.pbox_start = h->dpbox_start.p;
+    p.pbox_list = h->dpbox_list.p;
+    for (int k = 0; k < 3; k++) {
+      p.pbox_lo[k] = h->pgrid.lo[k];
+      p.pbox_inv[k] = h->pgrid.inv[k];
+      p.pbox_dims[k] = h->pgrid.dims[k];
+    }
+  }
   return p;
 }
 
@@ -577,6 +604,10 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->cell_start.free();
   h->tile_sums.free();
   h->pairs.free();
+  h->dpanels.free();
+  h->dsurf_act.free();
+  h->dpbox_start.free();
+  h->dpbox_list.free();
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return BD_OK;
@@ -629,6 +660,40 @@ BD_API bd_status bd_set_product_placement(bd_handle h, int rxn, int kind, float 
 
 namespace {
 // Pack every instance's derived parameters into the device blocks.
+static_assert(sizeof(bd_panel_info) <= sizeof(DevPanel), "DevPanel holds a bd_panel_info");
+
+uint8_t surface_action(const bd_system* h, int surf, int sp, int face) {
+  const bd_system::Surface& S = h->surfaces[surf];
+  const int v = sp < (int)S.species[face].size() ? S.species[face][sp] : -1;
+  return v >= 0 ? (uint8_t)v : S.all[face];
+}
+
+// [surface][species][front, back] actions for the kernels.
+std::vector<uint8_t> surface_table(const bd_system* h) {
+  const int S = (int)h->D.size();
+  std::vector<uint8_t> t(h->surfaces.size() * (size_t)S * 2);
+  for (size_t f = 0; f < h->surfaces.size(); f++)
+    for (int sp = 0; sp < S; sp++)
+      for (int face = 0; face < 2; face++) t[(f * S + sp) * 2 + face] = surface_action(h, (int)f, sp, face);
+  return t;
+}
+
+// The panel grid spans the union of the instances' boxes (positions outside
+// it map to its edge boxes, so any box is correct, only slower).
+void plan_panel_grid(bd_system* h) {
+  float lo[3], hi[3];
+  for (int k = 0; k < 3; k++) {
+    lo[k] = h->idesc[0].box_lo[k];
+    hi[k] = h->idesc[0].box_hi[k];
+  }
+  for (const bd_instance_desc& d : h->idesc)
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::min(lo[k], d.box_lo[k]);
+      hi[k] = std::max(hi[k], d.box_hi[k]);
+    }
+  build_panel_grid(h->panels, lo, hi, &h->pgrid);
+}
+
 bd_status pack_blocks(bd_system* h) {
   const int I = h->n_inst(), S = h->S, U = h->U, B = h->B, Z = h->Z;
   std::vector<DevSpecies> sp((size_t)I * S);
@@ -702,6 +767,17 @@ bd_status pack_blocks(bd_system* h) {
       (st = upload(h->dcdf, cdf, h->stream)) || (st = upload(h->dtable, h->bim_table, h->stream)) ||
       (st = upload(h->dgauss, gauss, h->stream)))
     return st;
+  if (!h->panels.empty()) {
+    std::vector<DevPanel> dp(h->panels.size());
+    for (size_t k = 0; k < dp.size(); k++) {
+      memset(&dp[k], 0, sizeof(DevPanel));
+      memcpy(&dp[k], &h->panels[k], sizeof(bd_panel_info));
+    }
+    if ((st = upload(h->dpanels, dp, h->stream)) || (st = upload(h->dsurf_act, surface_table(h), h->stream)) ||
+        (st = upload(h->dpbox_start, h->pgrid.start, h->stream)) ||
+        (st = upload(h->dpbox_list, h->pgrid.list, h->stream)))
+      return st;
+  }
   BD_CUDA(cudaStreamSynchronize(h->stream));
   return BD_OK;
 }
@@ -781,10 +857,79 @@ BD_API bd_status bd_finalize(bd_handle h) {
     e1 = b;
   }
 
+  if (!h->panels.empty()) plan_panel_grid(h);
   bd_status st = pack_blocks(h);
   if (st) return st;
   h->finalized = true;
   return first;
+}
+
+BD_API bd_status bd_add_surface(bd_handle h, int* surface) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (h->surfaces.size() >= 0x10000) return BD_ERR_CAPACITY;
+  h->surfaces.emplace_back();
+  if (surface) *surface = (int)h->surfaces.size() - 1;
+  return BD_OK;
+}
+
+BD_API bd_status bd_set_surface_action(bd_handle h, int surface, int species, int face, int action) {
+  if (!h || surface < 0 || surface >= (int)h->surfaces.size()) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (species != BD_ALL_SPECIES && (species < 0 || species >= (int)h->D.size())) return BD_ERR_INVALID_ARGUMENT;
+  if (face < BD_FACE_FRONT || face > BD_FACE_BOTH) return BD_ERR_INVALID_ARGUMENT;
+  if (action != BD_SURF_TRANSMIT && action != BD_SURF_REFLECT && action != BD_SURF_ABSORB)
+    return BD_ERR_INVALID_ARGUMENT;
+  bd_system::Surface& S = h->surfaces[surface];
+  for (int f = 0; f < 2; f++) {
+    if (face != BD_FACE_BOTH && face != f) continue;
+    if (species == BD_ALL_SPECIES) {
+      // a later "all" statement overrides the earlier per-species ones
+      S.all[f] = (uint8_t)action;
+      S.species[f].clear();
+    } else {
+      if ((int)S.species[f].size() <= species) S.species[f].resize(species + 1, -1);
+      S.species[f][species] = (int16_t)action;
+    }
+  }
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_surface_action(bd_handle h, int surface, int species, int face, int* action) {
+  if (!h || !action || surface < 0 || surface >= (int)h->surfaces.size()) return BD_ERR_INVALID_ARGUMENT;
+  if (species < 0 || species >= (int)h->D.size() || (face != BD_FACE_FRONT && face != BD_FACE_BACK))
+    return BD_ERR_INVALID_ARGUMENT;
+  *action = surface_action(h, surface, species, face);
+  return BD_OK;
+}
+
+BD_API bd_status bd_add_panel(bd_handle h, int surface, const bd_panel* panel, int* id) {
+  if (!h || !panel || surface < 0 || surface >= (int)h->surfaces.size()) return BD_ERR_INVALID_ARGUMENT;
+  if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
+  if (h->panels.size() >= (1u << 24)) return BD_ERR_CAPACITY;
+  bd_panel_info info;
+  std::string msg;
+  const bd_status st = derive_panel(*panel, surface, &info, &msg);
+  if (st) {
+    g_last_error = msg;
+    return st;
+  }
+  h->panels.push_back(info);
+  if (id) *id = (int)h->panels.size() - 1;
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_panel(bd_handle h, int id, bd_panel_info* out) {
+  if (!h || !out || id < 0 || id >= (int)h->panels.size()) return BD_ERR_INVALID_ARGUMENT;
+  *out = h->panels[id];
+  return BD_OK;
+}
+
+BD_API bd_status bd_get_surface_counts(bd_handle h, int* n_surfaces, int* n_panels) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  if (n_surfaces) *n_surfaces = (int)h->surfaces.size();
+  if (n_panels) *n_panels = (int)h->panels.size();
+  return BD_OK;
 }
 
 BD_API bd_status bd_get_counts(bd_handle h, int* n_species, int* n_reactions) {

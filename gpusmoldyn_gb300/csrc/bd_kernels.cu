@@ -35,6 +35,7 @@
 // are appended by k_append.
 #include "bd_device.cuh"
 #include "bd_kernels.h"
+#include "bd_surface.cuh"
 
 namespace bd {
 namespace {
@@ -149,7 +150,24 @@ __device__ __forceinline__ SingleCtx single_ctx(const KParams& p, DevSpecies* s_
 // first successful first-order reaction (reaction_kernel.cuh:303-341: coins
 // in list order, decay when the first product is absent, a second product
 // becomes a birth).  kCount adds fired reactions to the event counters.
-template <bool kTable, bool kCount, bool kSingle>
+// The surface walk of a move from x0 to (x, y, z), a point the walls have
+// already reflected into the box: the chord stays inside the box, so a panel
+// that reaches a wall cannot be passed by way of the wall.  A reflection off
+// a panel can leave the box, so the walls reflect the end once more.
+// False = absorbed.
+__device__ __forceinline__ bool surface_walk(const KParams& p, const DevInstance& I, uint32_t sp, const V3& x0,
+                                             float& x, float& y, float& z) {
+  V3 e{x, y, z};
+  if (!surface_move(surf_view(p), sp, x0, e)) return false;
+  x = reflect(e.x, I.lo[0], I.hi[0]);
+  y = reflect(e.y, I.lo[1], I.hi[1]);
+  z = reflect(e.z, I.lo[2], I.hi[2]);
+  return true;
+}
+
+// kSurf walks each displacement (the diffusion step, product offsets)
+// through the surface panels.
+template <bool kTable, bool kCount, bool kSingle, bool kSurf = false>
 __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& ctx, const float4 rec, uint32_t i,
                                             Out2& o) {
   o.n = 0;
@@ -176,6 +194,7 @@ __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& c
   float x = reflect(__fmaf_rn(S.sigma, g0, rec.x), I.lo[0], I.hi[0]);
   float y = reflect(__fmaf_rn(S.sigma, g1, rec.y), I.lo[1], I.hi[1]);
   float z = reflect(__fmaf_rn(S.sigma, g2, rec.z), I.lo[2], I.hi[2]);
+  if (kSurf && !surface_walk(p, I, sp, V3{rec.x, rec.y, rec.z}, x, y, z)) return;  // absorbed
   uint32_t species = sp;
   int n = 1;
 
@@ -190,19 +209,34 @@ __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& c
       species = (uint32_t)u.prod0;
       if (u.prod1 >= 0) {
         float bx = x, by = y, bz = z;
+        bool keep0 = true, keep1 = true;
         if (u.off0 != 0.0f || u.off1 != 0.0f) {
           float dx, dy, dz;
           unit_vector(local, t, kTagUniDir, 0u, k0, k1, dx, dy, dz);
           bx = reflect(__fmaf_rn(u.off1, dx, x), I.lo[0], I.hi[0]);
           by = reflect(__fmaf_rn(u.off1, dy, y), I.lo[1], I.hi[1]);
           bz = reflect(__fmaf_rn(u.off1, dz, z), I.lo[2], I.hi[2]);
+          const V3 from{x, y, z};
           x = reflect(__fmaf_rn(u.off0, dx, x), I.lo[0], I.hi[0]);
           y = reflect(__fmaf_rn(u.off0, dy, y), I.lo[1], I.hi[1]);
           z = reflect(__fmaf_rn(u.off0, dz, z), I.lo[2], I.hi[2]);
+          if (kSurf) {
+            // both products move from the reaction point
+            keep1 = surface_walk(p, I, (uint32_t)u.prod1, from, bx, by, bz);
+            keep0 = surface_walk(p, I, (uint32_t)u.prod0, from, x, y, z);
+          }
         }
-        o.r[1] = make_float4(bx, by, bz, __uint_as_float(pack_w(inst, (uint32_t)u.prod1) | kNewborn));
+        const float4 born = make_float4(bx, by, bz, __uint_as_float(pack_w(inst, (uint32_t)u.prod1) | kNewborn));
+        if (kSurf && !keep0) {  // the first product was absorbed: the birth takes its place
+          if (!keep1) return;
+          o.r[0] = born;
+          o.key[0] = cell_key(I, bx, by, bz);
+          o.n = 1;
+          return;
+        }
+        o.r[1] = born;
         o.key[1] = cell_key(I, bx, by, bz);
-        n = 2;
+        n = (kSurf && !keep1) ? 1 : 2;
       }
       break;
     }
@@ -338,7 +372,7 @@ __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
 
 // kMinBlocks 4 / 6 cap registers at 64 / 40 (50% / 75% occupancy, the
 // latter with a few spills); the launch shape picks the variant.
-template <bool kTable, int kMinBlocks, bool kSingle>
+template <bool kTable, int kMinBlocks, bool kSingle, bool kSurf = false>
 __global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
   __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
@@ -352,7 +386,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
   stream_records(st, n_real, n_total, [&](uint32_t i, const float4& rec) {
     Out2 o;
     o.n = 0;
-    if (i < n_real) advance_rec<kTable, true, kSingle>(p, ctx, rec, i, o);
+    if (i < n_real) advance_rec<kTable, true, kSingle, kSurf>(p, ctx, rec, i, o);
     else if (i < n_total) advance_virtual<kSingle>(p, i - n_real, o);
     warp_count(p.cell_count, o.n > 0 ? o.key[0] : kNoKey);
     if (__any_sync(kFull, o.n > 1)) warp_count(p.cell_count, o.n > 1 ? o.key[1] : kNoKey);
@@ -415,7 +449,7 @@ __global__ void __launch_bounds__(1024) k_scan_down(KParams p) {
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) p.cell_start[p.n_cells] = ld_u32(&c->n_sorted);
 }
 
-template <bool kTable, int kMinBlocks, bool kSingle>
+template <bool kTable, int kMinBlocks, bool kSingle, bool kSurf = false>
 __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
   __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
@@ -429,7 +463,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
   stream_records(st, n_real, n_total, [&](uint32_t i, const float4& rec) {
     Out2 o;
     o.n = 0;
-    if (i < n_real) advance_rec<kTable, false, kSingle>(p, ctx, rec, i, o);
+    if (i < n_real) advance_rec<kTable, false, kSingle, kSurf>(p, ctx, rec, i, o);
     else if (i < n_total) advance_virtual<kSingle>(p, i - n_real, o);
     const int kmax = __any_sync(kFull, o.n > 1) ? 2 : 1;
 #pragma unroll
@@ -486,7 +520,7 @@ __device__ __forceinline__ void claim_retire(const KParams& p, DevCtrl* c, const
 // the step's arithmetic runs once and nothing is recomputed.  First
 // products keep the deferred claim above; the rare second products (births)
 // claim and store at once.
-template <bool kTable, int kMinBlocks, bool kSingle>
+template <bool kTable, int kMinBlocks, bool kSingle, bool kSurf = false>
 __global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
   __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
@@ -505,7 +539,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
   stream_records(st, n_real, n_total, [&](uint32_t i, const float4& rec) {
     Out2 o;
     o.n = 0;
-    if (i < n_real) advance_rec<kTable, true, kSingle>(p, ctx, rec, i, o);
+    if (i < n_real) advance_rec<kTable, true, kSingle, kSurf>(p, ctx, rec, i, o);
     else if (i < n_total) advance_virtual<kSingle>(p, i - n_real, o);
     const PendingClaim next = claim_issue(p.cell_count, o.n > 0 ? o.key[0] : kNoKey, o.r[0]);
     if (__any_sync(kFull, o.n > 1)) claim_retire(p, c, claim_issue(p.cell_count, o.n > 1 ? o.key[1] : kNoKey, o.r[1]));
@@ -1024,6 +1058,7 @@ __device__ __forceinline__ void commit_events(const KParams& p) {
 // are those of the greedy scan in (lower slot, upper slot) order, found in
 // parallel as rounds of locally dominant pairs: a pair is taken when each
 // end's smallest undecided partner is the other end.
+template <bool kSurf>
 __global__ void __launch_bounds__(1024) k_match(KParams p) {
   __shared__ uint32_t s_more, s_deaths;
   DevCtrl* c = p.ctrl;
@@ -1103,24 +1138,26 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
                   dz);
     }
     uint32_t dead = 0;
-    float4 n1 = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kDead));
-    float4 n2 = n1;
-    if (br.prod0 >= 0) {
-      n1 = make_float4(reflect(__fmaf_rn(br.off0, dx, rx), I.lo[0], I.hi[0]),
-                       reflect(__fmaf_rn(br.off0, dy, ry), I.lo[1], I.hi[1]),
-                       reflect(__fmaf_rn(br.off0, dz, rz), I.lo[2], I.hi[2]),
-                       __uint_as_float(pack_w(inst, (uint32_t)br.prod0)));
-    } else {
-      ++dead;
-    }
-    if (br.prod1 >= 0) {
-      n2 = make_float4(reflect(__fmaf_rn(br.off1, dx, rx), I.lo[0], I.hi[0]),
-                       reflect(__fmaf_rn(br.off1, dy, ry), I.lo[1], I.hi[1]),
-                       reflect(__fmaf_rn(br.off1, dz, rz), I.lo[2], I.hi[2]),
-                       __uint_as_float(pack_w(inst, (uint32_t)br.prod1)));
-    } else {
-      ++dead;
-    }
+    const float4 none = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kDead));
+    float4 n1 = none, n2 = none;
+    // each product moves from the reaction point by its offset, through the
+    // surfaces when there are any, then the walls
+    auto place = [&](int32_t prod, float off, float4& out) {
+      if (prod < 0) {
+        ++dead;
+        return;
+      }
+      float ex = reflect(__fmaf_rn(off, dx, rx), I.lo[0], I.hi[0]);
+      float ey = reflect(__fmaf_rn(off, dy, ry), I.lo[1], I.hi[1]);
+      float ez = reflect(__fmaf_rn(off, dz, rz), I.lo[2], I.hi[2]);
+      if (kSurf && off != 0.0f && !surface_walk(p, I, (uint32_t)prod, V3{rx, ry, rz}, ex, ey, ez)) {
+        ++dead;
+        return;
+      }
+      out = make_float4(ex, ey, ez, __uint_as_float(pack_w(inst, (uint32_t)prod)));
+    };
+    place(br.prod0, br.off0, n1);
+    place(br.prod1, br.off1, n2);
     nx[m1] = n1;
     nx[m2] = n2;
     atomicAdd(&p.pending[(size_t)inst * p.R + br.rxn], 1ull);
@@ -1271,13 +1308,28 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
       else KERNEL<false, MINB, false><<<gs, bs, 0, s>>>(p);                                 \
     }                                                                                      \
   } while (0)
-#define BD_STREAM_LAUNCH(KERNEL)                   \
-  do {                                             \
-    switch (shape.min_blocks) {                    \
-      case 6: BD_STREAM_LAUNCH3(KERNEL, 6); break; \
-      case 4: BD_STREAM_LAUNCH3(KERNEL, 4); break; \
-      default: BD_STREAM_LAUNCH3(KERNEL, 1);       \
-    }                                              \
+  // With surfaces: one variant per kernel, no register cap.
+#define BD_STREAM_LAUNCH_SURF(KERNEL)                                                      \
+  do {                                                                                     \
+    if (single) {                                                                          \
+      if (table) KERNEL<true, 1, true, true><<<gs, bs, 0, s>>>(p);                          \
+      else KERNEL<false, 1, true, true><<<gs, bs, 0, s>>>(p);                               \
+    } else {                                                                               \
+      if (table) KERNEL<true, 1, false, true><<<gs, bs, 0, s>>>(p);                         \
+      else KERNEL<false, 1, false, true><<<gs, bs, 0, s>>>(p);                              \
+    }                                                                                      \
+  } while (0)
+#define BD_STREAM_LAUNCH(KERNEL)                     \
+  do {                                               \
+    if (p.n_panels) {                                \
+      BD_STREAM_LAUNCH_SURF(KERNEL);                 \
+    } else {                                         \
+      switch (shape.min_blocks) {                    \
+        case 6: BD_STREAM_LAUNCH3(KERNEL, 6); break; \
+        case 4: BD_STREAM_LAUNCH3(KERNEL, 4); break; \
+        default: BD_STREAM_LAUNCH3(KERNEL, 1);       \
+      }                                              \
+    }                                                \
   } while (0)
 #define BD_PAIRS_LAUNCH(BINNED)                                                                      \
   do {                                                                                               \
@@ -1307,7 +1359,8 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
       k_pairs_big_pairs<true, true><<<kBigGrid, 256, 0, s>>>(p);
       done("k_pairs_big_pairs");
     }
-    k_match<<<1, 1024, 0, s>>>(p);
+    if (p.n_panels) k_match<true><<<1, 1024, 0, s>>>(p);
+    else k_match<false><<<1, 1024, 0, s>>>(p);
     done("k_match");
     return n;
   }
@@ -1323,6 +1376,7 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   done("k_scatter");
   BD_PAIRS_LAUNCH(false);
 #undef BD_STREAM_LAUNCH
+#undef BD_STREAM_LAUNCH_SURF
 #undef BD_STREAM_LAUNCH3
 #undef BD_PAIRS_LAUNCH
   done("k_pairs_cells");
@@ -1332,7 +1386,8 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     k_pairs_big_pairs<true, false><<<kBigGrid, 256, 0, s>>>(p);
     done("k_pairs_big_pairs");
   }
-  k_match<<<1, 1024, 0, s>>>(p);
+  if (p.n_panels) k_match<true><<<1, 1024, 0, s>>>(p);
+  else k_match<false><<<1, 1024, 0, s>>>(p);
   done("k_match");
   return n;
 }

@@ -42,6 +42,14 @@ struct KParams {
   float4* big_scratch;        // [big_scratch_cap] merge-sort buffer of k_pairs_big
   uint32_t big_cap, big_scratch_cap;
   float prune_margin;         // fraction of a cell edge added to pruning distances
+  // surfaces (n_panels = 0: none)
+  const DevPanel* panels;     // [n_panels]
+  const uint8_t* surf_act;    // [n_surfaces][S][2] SurfaceAction per (species, front/back face)
+  const uint32_t* pbox_start; // [n_pbox + 1] panel lists of the coarse panel grid
+  const uint32_t* pbox_list;  // panel ids, box by box
+  float pbox_lo[3], pbox_inv[3];
+  uint32_t pbox_dims[3];
+  uint32_t n_panels;
 };
 
 // kSorted: counting sort into compact cell ranges (k_count, scans,

@@ -122,6 +122,28 @@ enum StatusBits : uint32_t {
   kStatScratch = 32u,      // the large-cell kernel needs its sort buffer
 };
 
+// Surface panels.  The shape codes and the field meanings are those of the
+// public bd_panel_info (one float/int per field, same order), so the host
+// fills a DevPanel by copying a bd_panel_info.
+enum PanelShape : uint32_t { kPanelRect = 0, kPanelTri = 1, kPanelSph = 2, kPanelCyl = 3, kPanelHemi = 4,
+                             kPanelDisk = 5 };
+enum SurfaceAction : uint8_t { kActTransmit = 0, kActReflect = 1, kActAbsorb = 2 };
+constexpr int kMaxSurfaceHits = 8;  // crossings handled per segment and step
+
+struct DevPanel {          // 96 B
+  uint32_t shape;          // PanelShape
+  uint32_t surface;        // owning surface (index of its action table)
+  uint32_t axis;           // rect: axis perpendicular to the panel
+  float front;             // +1 / -1: which way the front face looks
+  float a[3];              // rect corner, tri v0, sph/hemi/disk centre, cyl end 0
+  float r, r2;             // radius and its square
+  float n[3];              // tri/disk unit front normal, cyl unit axis, hemi unit opening direction
+  float len;               // cyl axis length
+  float v1[3], v2[3];      // tri vertices 1 and 2
+  float bounds[4];         // rect: lower in-plane axis lo, hi; higher one lo, hi
+  uint32_t pad;
+};
+
 // Pair list entry written by the pair kernel and resolved by the matcher.
 struct DevPair {           // 16 B
   uint32_t i, j;           // canonical slots, i < j

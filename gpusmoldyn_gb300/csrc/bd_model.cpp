@@ -9,7 +9,7 @@
 //   boundaries <axis> <low> <high> [r]       axis 0|1|2|x|y|z, reflecting walls
 //   low_wall <axis> <pos> r / high_wall <axis> <pos> r
 //   species <name> ...
-//   difc <species>[(state)] <D>
+//   difc <species>[(state)]|all <D>
 //   time_start <t> / time_stop <t> / time_step <dt>
 //   random_seed <n>
 //   reaction <name> <r1> [+ <r2>] -> <p1> [+ <p2>] <rate>     "0" = none
@@ -17,6 +17,17 @@
 //   reaction_probability <name> <p>
 //   product_placement <name> irrev|pgem|pgemmax|unbindrad [<value>]
 //   mol <count> <species> <x|u> <y|u> <z|u>  u = uniform in the box
+//   start_surface <name> ... end_surface, with inside:
+//     action <species|all> <front|back|both> <reflect|absorb|transmit>
+//       (the face may also come first)
+//     panel rect <+-axis> <x> <y> <z> <side1> <side2>
+//     panel tri <x1> <y1> <z1> <x2> <y2> <z2> <x3> <y3> <z3>
+//     panel sph <x> <y> <z> <radius>                     (radius < 0: front inside)
+//     panel cyl <x1> <y1> <z1> <x2> <y2> <z2> <radius>   (radius < 0: front inside)
+//     panel hemi <x> <y> <z> <radius> <ox> <oy> <oz>     (radius < 0: front inside)
+//     panel disk <x> <y> <z> <radius> <nx> <ny> <nz>
+//     (drawing parameters and panel names after these are ignored)
+//   surface <name> <statement>                 one surface statement outside a block
 //   end_file
 // Display, output and runtime-command statements (graphics, output_files,
 // cmd, ...) are accepted and ignored; anything else is an error naming the
@@ -34,6 +45,7 @@
 #include <vector>
 
 #include "../../include/gpusmoldyn.h"
+#include "bd_surface.h"
 
 namespace {
 
@@ -52,17 +64,29 @@ struct MolStmt {
   int line = 0;
 };
 
+struct ActionStmt {
+  std::string species;  // "all" = every species
+  int face = BD_FACE_BOTH, action = BD_SURF_REFLECT, line = 0;
+};
+
+struct SurfaceStmt {
+  std::string name;
+  std::vector<ActionStmt> actions;
+  std::vector<std::pair<bd_panel, int>> panels;  // panel, line
+};
+
 struct Model {
   double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
   bool axis_set[3] = {false, false, false};
   double dt = 0.0, t_start = 0.0, t_stop = 0.0;
   uint64_t seed = 1;
   std::vector<std::string> species;
-  std::map<std::string, double> difc;
+  std::vector<std::pair<std::string, double>> difc;  // in order; "all" = every species
   std::vector<RxnStmt> rxns;
   std::map<std::string, double> probability;
   std::map<std::string, std::pair<std::string, double>> placement;
   std::vector<MolStmt> mols;
+  std::vector<SurfaceStmt> surfaces;
 };
 
 const char* const kIgnored[] = {
@@ -112,11 +136,107 @@ struct Failure {
     throw Failure{(code), _m.str()};                                     \
   } while (0)
 
+// Display statements of a surface block.
+bool surface_display(const std::string& k) {
+  return k == "color" || k == "colour" || k == "thickness" || k == "stipple" || k == "polygon" ||
+         k == "shininess" || k == "max_panels";
+}
+
+SurfaceStmt& surface_named(Model& m, const std::string& name) {
+  for (SurfaceStmt& f : m.surfaces)
+    if (f.name == name) return f;
+  m.surfaces.push_back(SurfaceStmt{});
+  m.surfaces.back().name = name;
+  return m.surfaces.back();
+}
+
+// One statement of a surface block, w[0] its keyword.
+void surface_statement(SurfaceStmt& f, const std::vector<std::string>& w, int ln) {
+  const std::string& k = w[0];
+  if (surface_display(k)) return;
+  if (k == "action") {
+    if (w.size() != 4) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "action <species|all> <front|back|both> <action>");
+    auto face_of = [](const std::string& t, int* face) {
+      if (t == "front") *face = BD_FACE_FRONT;
+      else if (t == "back") *face = BD_FACE_BACK;
+      else if (t == "both") *face = BD_FACE_BOTH;
+      else return false;
+      return true;
+    };
+    ActionStmt a;
+    a.line = ln;
+    if (face_of(w[1], &a.face)) {
+      a.species = base_name(w[2]);
+    } else if (face_of(w[2], &a.face)) {
+      a.species = base_name(w[1]);
+    } else {
+      FAIL(BD_ERR_INVALID_ARGUMENT, ln, "action needs a face: front, back or both");
+    }
+    const std::string& t = w[3];
+    if (t == "reflect" || t == "r") a.action = BD_SURF_REFLECT;
+    else if (t == "absorb" || t == "a") a.action = BD_SURF_ABSORB;
+    else if (t == "transmit" || t == "t") a.action = BD_SURF_TRANSMIT;
+    else FAIL(BD_ERR_UNSUPPORTED, ln, "surface action " << t << " is not supported (reflect, absorb, transmit)");
+    f.actions.push_back(a);
+    return;
+  }
+  if (k == "panel") {
+    if (w.size() < 2) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "panel <shape> <parameters>");
+    bd_panel pn{};
+    pn.front = 1;
+    const std::string& shape = w[1];
+    size_t need = 0, first = 2;
+    if (shape == "rect") {
+      // "+0", "-x", "+y", ...: the perpendicular axis and the way the front looks
+      if (w.size() < 3 || w[2].size() != 2 || (w[2][0] != '+' && w[2][0] != '-') ||
+          !parse_axis(w[2].substr(1), &pn.axis))
+        FAIL(BD_ERR_INVALID_ARGUMENT, ln, "panel rect <+-axis> <x> <y> <z> <side1> <side2>");
+      pn.front = w[2][0] == '+' ? 1 : -1;
+      pn.shape = BD_PANEL_RECT;
+      need = 5;
+      first = 3;
+    } else if (shape == "tri") {
+      pn.shape = BD_PANEL_TRI;
+      need = 9;
+    } else if (shape == "sph") {
+      pn.shape = BD_PANEL_SPH;
+      need = 4;
+    } else if (shape == "cyl") {
+      pn.shape = BD_PANEL_CYL;
+      need = 7;
+    } else if (shape == "hemi") {
+      pn.shape = BD_PANEL_HEMI;
+      need = 7;
+    } else if (shape == "disk") {
+      pn.shape = BD_PANEL_DISK;
+      need = 7;
+    } else {
+      FAIL(BD_ERR_UNSUPPORTED, ln, "panel shape " << shape << " is not supported");
+    }
+    if (w.size() < first + need) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "panel " << shape << " needs " << need << " numbers");
+    for (size_t i = 0; i < need; i++) {
+      double v;
+      if (!parse_num(w[first + i], &v)) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "bad number " << w[first + i]);
+      pn.p[i] = (float)v;
+    }
+    // a negative radius turns the front face inward
+    const int ri = shape == "cyl" ? 6 : 3;
+    if ((shape == "sph" || shape == "cyl" || shape == "hemi") && pn.p[ri] < 0) {
+      pn.p[ri] = -pn.p[ri];
+      pn.front = -1;
+    }
+    f.panels.push_back({pn, ln});
+    return;
+  }
+  FAIL(BD_ERR_UNSUPPORTED, ln, "surface statement " << k << " is not supported");
+}
+
 Model parse(const std::string& text) {
   Model m;
   std::istringstream in(text);
   std::string raw;
   int ln = 0;
+  SurfaceStmt* block = nullptr;  // inside start_surface .. end_surface
   while (std::getline(in, raw)) {
     ++ln;
     const size_t hash = raw.find('#');
@@ -128,8 +248,19 @@ Model parse(const std::string& text) {
     const std::string& k = w[0];
     double v;
     if (k == "end_file") break;
-    if (ignored(k)) continue;
-    if (k == "dim") {
+    if (block) {
+      if (k == "end_surface") block = nullptr;
+      else surface_statement(*block, w, ln);
+      continue;
+    }
+    if (ignored(k) || k == "max_surface") continue;
+    if (k == "start_surface") {
+      if (w.size() != 2) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "start_surface <name>");
+      block = &surface_named(m, w[1]);
+    } else if (k == "surface") {
+      if (w.size() < 3) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "surface <name> <statement>");
+      surface_statement(surface_named(m, w[1]), std::vector<std::string>(w.begin() + 2, w.end()), ln);
+    } else if (k == "dim") {
       if (w.size() != 2 || w[1] != "3") FAIL(BD_ERR_UNSUPPORTED, ln, "only dim 3 is supported");
     } else if (k == "boundaries") {
       int a;
@@ -156,7 +287,7 @@ Model parse(const std::string& text) {
       }
     } else if (k == "difc") {
       if (w.size() != 3 || !parse_num(w[2], &v) || v < 0) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "difc <species> <D>");
-      m.difc[base_name(w[1])] = v;
+      m.difc.push_back({base_name(w[1]), v});
     } else if (k == "time_start" || k == "time_stop" || k == "time_step") {
       if (w.size() != 2 || !parse_num(w[1], &v)) FAIL(BD_ERR_INVALID_ARGUMENT, ln, k << " <value>");
       (k == "time_start" ? m.t_start : (k == "time_stop" ? m.t_stop : m.dt)) = v;
@@ -225,6 +356,7 @@ Model parse(const std::string& text) {
       FAIL(BD_ERR_INVALID_ARGUMENT, ln, "unknown statement '" << k << "'");
     }
   }
+  if (block) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "start_surface " << block->name << " without end_surface");
   for (int a = 0; a < 3; a++)
     if (!m.axis_set[a] || !(m.hi[a] > m.lo[a])) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "boundaries missing for axis " << a);
   if (!(m.dt > 0)) FAIL(BD_ERR_INVALID_ARGUMENT, ln, "time_step missing");
@@ -262,13 +394,16 @@ bd_handle build(const Model& m, int device, bd_model_info* info) {
   bd_handle h = nullptr;
   check(bd_create(&cfg, &h), 0, "bd_create");
   try {
+    std::vector<double> D(m.species.size(), 0.0);
+    for (const auto& d : m.difc) {
+      if (d.first == "all") D.assign(D.size(), d.second);
+      else D[species_id(m, d.first, 0)] = d.second;
+    }
     for (size_t i = 0; i < m.species.size(); i++) {
-      const auto d = m.difc.find(m.species[i]);
       int id;
-      check(bd_add_species(h, d == m.difc.end() ? 0.0f : (float)d->second, &id), 0, "species");
+      check(bd_add_species(h, (float)D[i], &id), 0, "species");
       check(bd_set_species_name(h, id, m.species[i].c_str()), 0, "species name");
     }
-    for (const auto& d : m.difc) species_id(m, d.first, 0);
     for (const RxnStmt& r : m.rxns) {
       if (!r.has_rate) FAIL(BD_ERR_INVALID_ARGUMENT, r.line, "reaction " << r.name << " has no rate");
       int rc[2] = {-1, -1}, pr[2] = {-1, -1};
@@ -295,6 +430,20 @@ bd_handle build(const Model& m, int device, bd_model_info* info) {
       if (bd_find_reaction(h, pr.first.c_str(), &rx_id) != BD_OK)
         FAIL(BD_ERR_INVALID_ARGUMENT, 0, "reaction_probability of unknown reaction " << pr.first);
       check(bd_set_reaction_probability(h, rx_id, (float)pr.second), 0, "reaction_probability");
+    }
+    for (const SurfaceStmt& f : m.surfaces) {
+      int sid;
+      check(bd_add_surface(h, &sid), 0, "surface");
+      for (const ActionStmt& a : f.actions) {
+        const int sp = a.species == "all" ? BD_ALL_SPECIES : species_id(m, a.species, a.line);
+        check(bd_set_surface_action(h, sid, sp, a.face, a.action), a.line, "action");
+      }
+      for (const auto& pl : f.panels) {
+        bd_panel_info probe;
+        std::string why;
+        if (bd::derive_panel(pl.first, sid, &probe, &why)) FAIL(BD_ERR_INVALID_ARGUMENT, pl.second, "panel: " << why);
+        check(bd_add_panel(h, sid, &pl.first, nullptr), pl.second, "panel");
+      }
     }
     check(bd_finalize(h), 0, "finalize");
     uint64_t n = 0;

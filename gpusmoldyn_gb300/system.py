@@ -135,6 +135,58 @@ class System:
     def set_reaction_probability(self, rxn, prob):
         L.check(self.lib.bd_set_reaction_probability(self.h, rxn, prob), "bd_set_reaction_probability")
 
+    # surfaces
+    _FACES = {"front": L.BD_FACE_FRONT, "back": L.BD_FACE_BACK, "both": L.BD_FACE_BOTH}
+    _ACTIONS = {"transmit": L.BD_SURF_TRANSMIT, "reflect": L.BD_SURF_REFLECT, "absorb": L.BD_SURF_ABSORB}
+    _SHAPES = {"rect": L.BD_PANEL_RECT, "tri": L.BD_PANEL_TRI, "sph": L.BD_PANEL_SPH, "cyl": L.BD_PANEL_CYL,
+               "hemi": L.BD_PANEL_HEMI, "disk": L.BD_PANEL_DISK}
+
+    def add_surface(self) -> int:
+        i = C.c_int()
+        L.check(self.lib.bd_add_surface(self.h, C.byref(i)), "bd_add_surface")
+        return i.value
+
+    def set_surface_action(self, surface, species=L.BD_ALL_SPECIES, face="both", action="reflect"):
+        """species: id or BD_ALL_SPECIES; face and action by name or BD_* code."""
+        face = self._FACES.get(face, face)
+        action = self._ACTIONS.get(action, action)
+        L.check(self.lib.bd_set_surface_action(self.h, surface, species, face, action), "bd_set_surface_action")
+
+    def surface_action(self, surface, species, face) -> int:
+        v = C.c_int()
+        L.check(self.lib.bd_get_surface_action(self.h, surface, species, self._FACES.get(face, face), C.byref(v)),
+                "bd_get_surface_action")
+        return v.value
+
+    def add_panel(self, surface, shape, params, axis=0, front=1) -> int:
+        """One panel of `surface`: shape by name or BD_PANEL_* code, params as
+        in bd_panel.p (rect: corner, two sides; tri: 3 vertices; sph: centre,
+        radius; cyl: two ends, radius; hemi: centre, radius, opening
+        direction; disk: centre, radius, normal)."""
+        pn = L.bd_panel()
+        pn.shape = self._SHAPES.get(shape, shape)
+        pn.axis = axis
+        pn.front = front
+        vals = list(params)
+        if len(vals) > 10:
+            raise ValueError("at most 10 panel parameters")
+        for k, v in enumerate(vals):
+            pn.p[k] = v
+        i = C.c_int()
+        L.check(self.lib.bd_add_panel(self.h, surface, C.byref(pn), C.byref(i)), "bd_add_panel")
+        return i.value
+
+    def panel_info(self, pid) -> dict:
+        q = L.bd_panel_info()
+        L.check(self.lib.bd_get_panel(self.h, pid, C.byref(q)), "bd_get_panel")
+        return {name: (list(getattr(q, name)) if hasattr(getattr(q, name), "__len__") else getattr(q, name))
+                for name, _ in L.bd_panel_info._fields_}
+
+    def surface_counts(self):
+        ns, npn = C.c_int(), C.c_int()
+        L.check(self.lib.bd_get_surface_counts(self.h, C.byref(ns), C.byref(npn)), "bd_get_surface_counts")
+        return ns.value, npn.value
+
     def finalize(self, allow=(L.BD_OK, L.BD_ERR_PGEM_UNATTAINABLE)):
         st = self.lib.bd_finalize(self.h)
         L.check(st, "bd_finalize", ok=allow)

@@ -352,6 +352,81 @@ BD_API bd_status bd_instance_state(bd_handle h, int slot, uint32_t *steps, uint3
 BD_API bd_status bd_cell_sort_static(const float *d_in, uint64_t n, const float box_lo[3], const float box_hi[3],
                                      const uint32_t dims[3], float *d_out, uint32_t *d_cell_start, void *stream);
 
+/* ------------------------------------------------------------ surfaces */
+/* Surfaces made of panels that reflect, absorb or transmit molecules, per
+ * species and per face (Smoldyn's surfaces).  The reference only drafts
+ * them: panel geometry and the crossing test in surfaces_kernel.cuh:97-248,
+ * a per-cell panel walk in checkSurfaceCollisions (particles_kernel.cu:
+ * 414-440) that is never launched and does not compile.  Here every step
+ * tests the segment from a molecule's old position to its diffused one
+ * against the panels (found through a coarse grid of panel lists), takes
+ * the first crossing along it and applies the surface's action for the
+ * molecule's species on the face it arrives from: ABSORB removes it,
+ * TRANSMIT lets it through, REFLECT mirrors the rest of the step in the
+ * panel's tangent plane at the crossing point; the walk continues with what
+ * is left of the segment (at most 8 crossings a step, after which the
+ * molecule stays at its last crossing point).  The box walls reflect after
+ * the surfaces.  The segments from a reaction point to its displaced
+ * products are tested the same way.  Pairs react whatever panel lies
+ * between them, and zeroth-order births are uniform in the box.  A panel
+ * whose surface transmits a species on both faces (the default action) is
+ * invisible to that species.  Surfaces and panels are added before
+ * bd_finalize; panels are shared by all instances of an ensemble, in each
+ * instance's coordinates. */
+enum {
+  BD_PANEL_RECT = 0,  /* axis-aligned rectangle */
+  BD_PANEL_TRI = 1,   /* triangle */
+  BD_PANEL_SPH = 2,   /* sphere */
+  BD_PANEL_CYL = 3,   /* open cylinder (no end caps) */
+  BD_PANEL_HEMI = 4,  /* hemisphere */
+  BD_PANEL_DISK = 5   /* flat disk */
+};
+enum { BD_FACE_FRONT = 0, BD_FACE_BACK = 1, BD_FACE_BOTH = 2 };
+enum { BD_SURF_TRANSMIT = 0, BD_SURF_REFLECT = 1, BD_SURF_ABSORB = 2 };
+#define BD_ALL_SPECIES (-1)
+
+/* One panel as given.  p[] by shape:
+ *   RECT  corner x, y, z; side along the lower-numbered other axis; side along
+ *         the higher-numbered one (sides may be negative).  axis = the axis the
+ *         rectangle is perpendicular to; front = +1: the front face looks
+ *         toward +axis, -1 toward -axis.
+ *   TRI   vertices v0, v1, v2; the front face is the one (v1-v0) x (v2-v0)
+ *         points to.
+ *   SPH   centre, radius.  front = +1: the front face is outside, -1 inside.
+ *   CYL   axis end 0, axis end 1, radius; front as SPH.
+ *   HEMI  centre, radius, opening direction (the shell is the half of the
+ *         sphere away from it); front as SPH.
+ *   DISK  centre, radius, normal (the front face is the one it points to).
+ * Points exactly on a panel belong to its back face. */
+typedef struct bd_panel {
+  int shape;
+  int axis;
+  int front;
+  float p[10];
+} bd_panel;
+
+/* The geometry a step uses for one panel, derived from bd_panel in float
+ * (unit normals, squared radius, rectangle bounds). */
+typedef struct bd_panel_info {
+  int shape, surface, axis;
+  float front;                /* +1 / -1 (RECT, SPH, CYL, HEMI) */
+  float a[3];                 /* RECT corner, TRI v0, SPH/HEMI/DISK centre, CYL end 0 */
+  float r, r2;                /* radius and its square */
+  float n[3];                 /* TRI, DISK unit front normal; CYL unit axis; HEMI unit opening direction */
+  float len;                  /* CYL axis length */
+  float v1[3], v2[3];         /* TRI vertices 1 and 2 */
+  float bounds[4];            /* RECT: lower axis lo, hi; higher axis lo, hi */
+} bd_panel_info;
+
+BD_API bd_status bd_add_surface(bd_handle h, int *surface);
+/* species = BD_ALL_SPECIES for every species defined so far; face one of
+ * BD_FACE_*; action one of BD_SURF_*.  The default is TRANSMIT. */
+BD_API bd_status bd_set_surface_action(bd_handle h, int surface, int species, int face, int action);
+BD_API bd_status bd_get_surface_action(bd_handle h, int surface, int species, int face, int *action);
+BD_API bd_status bd_add_panel(bd_handle h, int surface, const bd_panel *panel, int *id);
+BD_API bd_status bd_get_panel(bd_handle h, int id, bd_panel_info *out);
+BD_API bd_status bd_get_surface_counts(bd_handle h, int *n_surfaces, int *n_panels);
+
 /* ----------------------------------------------------------- snapshots */
 /* The molecules written to a file (no display: replaces the reference's
  * OpenGL viewer, render_particles.cpp / particles.cpp).  TEXT: "# step s

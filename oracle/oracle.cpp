@@ -128,6 +128,240 @@ void direction(const Rng& g, uint32_t a, uint32_t b, uint32_t tag, uint32_t d, f
   v[2] = 1.0f;
 }
 
+// ---- surfaces -------------------------------------------------------------
+// Smoldyn's surface panels (the reference drafts panelside / lineXpanel in
+// surfaces_kernel.cuh:97-248 and a per-molecule walk in
+// checkSurfaceCollisions, particles_kernel.cu:414-440, neither of which is
+// ever compiled).  A molecule's move x0 -> x1 is tested against every
+// panel; the first crossing along it (lowest fraction, then lowest panel id)
+// is acted on with the action of the panel's surface for the species on the
+// face the move arrives from: absorb ends the walk, transmit continues just
+// past the crossing, reflect mirrors the end in the tangent plane at the
+// crossing point and continues just before it; at most 8 crossings, after
+// which the molecule stays at its last crossing.  A surface that transmits
+// a species on both faces is invisible to it.  A point exactly on a panel
+// is on its back face.
+enum { P_RECT = 0, P_TRI = 1, P_SPH = 2, P_CYL = 3, P_HEMI = 4, P_DISK = 5 };
+
+inline float dot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+inline void diff3(const float a[3], const float b[3], float out[3]) {
+  for (int k = 0; k < 3; k++) out[k] = a[k] - b[k];
+}
+// component of w across the unit axis n
+inline void across(const float w[3], const float n[3], float out[3]) {
+  const float t = dot3(w, n);
+  for (int k = 0; k < 3; k++) out[k] = w[k] - t * n[k];
+}
+inline float clamp01(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
+
+float side(const or_panel& P, const float x[3]) {
+  float w[3];
+  diff3(x, P.a, w);
+  float s;
+  if (P.shape == P_RECT) {
+    s = x[P.axis] - P.a[P.axis];
+    return P.front > 0.0f ? s : -s;
+  }
+  if (P.shape == P_TRI || P.shape == P_DISK) return dot3(w, P.n);
+  if (P.shape == P_CYL) {
+    float q[3];
+    across(w, P.n, q);
+    s = dot3(q, q) - P.r2;
+  } else {
+    s = dot3(w, w) - P.r2;
+  }
+  return P.front > 0.0f ? s : -s;
+}
+
+// ((e x w) . n)
+float edge(const float e[3], const float w[3], const float n[3]) {
+  const float c[3] = {e[1] * w[2] - e[2] * w[1], e[2] * w[0] - e[0] * w[2], e[0] * w[1] - e[1] * w[0]};
+  return dot3(c, n);
+}
+
+bool on_curved(const or_panel& P, const float c[3]) {
+  if (P.shape == P_SPH) return true;
+  float w[3];
+  diff3(c, P.a, w);
+  const float h = dot3(w, P.n);
+  return P.shape == P_HEMI ? h <= 0.0f : (h >= 0.0f && h <= P.len);
+}
+
+bool crossing(const or_panel& P, const float x0[3], const float x1[3], float s0, float s1, float* t, bool* ff) {
+  const bool f0 = s0 > 0.0f, f1 = s1 > 0.0f;
+  float d[3], c[3];
+  diff3(x1, x0, d);
+  auto at = [&](float tt) {
+    for (int k = 0; k < 3; k++) c[k] = std::fmaf(tt, d[k], x0[k]);
+  };
+  if (P.shape == P_RECT || P.shape == P_TRI || P.shape == P_DISK) {
+    if (f0 == f1) return false;
+    *t = s0 / (s0 - s1);
+    *ff = f0;
+    at(*t);
+    if (P.shape == P_RECT) {
+      const int u = P.axis == 0 ? 1 : 0, v = P.axis == 2 ? 1 : 2;
+      return P.bounds[0] <= c[u] && c[u] <= P.bounds[1] && P.bounds[2] <= c[v] && c[v] <= P.bounds[3];
+    }
+    float w[3];
+    if (P.shape == P_DISK) {
+      diff3(c, P.a, w);
+      return dot3(w, w) <= P.r2;
+    }
+    float e[3];
+    diff3(P.v1, P.a, e);
+    diff3(c, P.a, w);
+    if (!(edge(e, w, P.n) >= 0.0f)) return false;
+    diff3(P.v2, P.v1, e);
+    diff3(c, P.v1, w);
+    if (!(edge(e, w, P.n) >= 0.0f)) return false;
+    diff3(P.a, P.v2, e);
+    diff3(c, P.v2, w);
+    return edge(e, w, P.n) >= 0.0f;
+  }
+  const bool outward = P.front > 0.0f;
+  const bool in0 = f0 != outward, in1 = f1 != outward;
+  if (in0 && in1) return false;
+  float w[3], A, B, C;
+  diff3(x0, P.a, w);
+  if (P.shape == P_CYL) {
+    float dq[3], wq[3];
+    across(d, P.n, dq);
+    across(w, P.n, wq);
+    A = dot3(dq, dq);
+    B = dot3(dq, wq);
+    C = dot3(wq, wq) - P.r2;
+  } else {
+    A = dot3(d, d);
+    B = dot3(d, w);
+    C = dot3(w, w) - P.r2;
+  }
+  if (!(A > 0.0f)) return false;
+  const float disc = B * B - A * C;
+  if (!in0 && !in1 && !(disc > 0.0f)) return false;
+  const float sq = std::sqrt(disc > 0.0f ? disc : 0.0f);
+  const float near = (-B - sq) / A, far = (-B + sq) / A;
+  if (in0 || in1) {
+    // one end inside: leaving through the far root or entering through the near one
+    *t = clamp01(in0 ? far : near);
+    *ff = f0;
+    at(*t);
+    return on_curved(P, c);
+  }
+  if (!(near >= 0.0f && near <= 1.0f)) return false;
+  *t = near;
+  *ff = f0;
+  at(near);
+  if (on_curved(P, c)) return true;
+  if (P.shape == P_SPH) return false;
+  *t = clamp01(far);
+  *ff = !f0;
+  at(*t);
+  return on_curved(P, c);
+}
+
+// unit normal toward the front face at c
+bool normal_at(const or_panel& P, const float c[3], float m[3]) {
+  if (P.shape == P_RECT) {
+    for (int k = 0; k < 3; k++) m[k] = k == P.axis ? P.front : 0.0f;
+    return true;
+  }
+  if (P.shape == P_TRI || P.shape == P_DISK) {
+    for (int k = 0; k < 3; k++) m[k] = P.n[k];
+    return true;
+  }
+  float w[3];
+  diff3(c, P.a, w);
+  if (P.shape == P_CYL) {
+    float q[3];
+    across(w, P.n, q);
+    for (int k = 0; k < 3; k++) w[k] = q[k];
+  }
+  const float L = std::sqrt(dot3(w, w));
+  if (!(L > 0.0f)) return false;
+  const float inv = P.front / L;
+  for (int k = 0; k < 3; k++) m[k] = w[k] * inv;
+  return true;
+}
+
+void mirror(const or_panel& P, const float c[3], float x1[3]) {
+  if (P.shape == P_RECT) {
+    x1[P.axis] = 2.0f * P.a[P.axis] - x1[P.axis];
+    return;
+  }
+  float m[3], v[3];
+  if (!normal_at(P, c, m)) return;
+  diff3(x1, c, v);
+  const float k2 = -2.0f * dot3(v, m);
+  for (int k = 0; k < 3; k++) x1[k] = std::fmaf(k2, m[k], x1[k]);
+}
+
+// a point on face `front` near c: c, else c pushed along the normal by
+// 2^-21 (|c|_1 + 1) x 1, 4, 16, ...; false if 8 pushes do not get there
+bool onto_face(const or_panel& P, const float c[3], bool front, float q[3]) {
+  for (int k = 0; k < 3; k++) q[k] = c[k];
+  if ((side(P, c) > 0.0f) == front) return true;
+  float m[3];
+  if (!normal_at(P, c, m)) return false;
+  float e = (((std::fabs(c[0]) + std::fabs(c[1])) + std::fabs(c[2])) + 1.0f) * 4.76837158203125e-07f;
+  if (!front) e = -e;
+  for (int it = 0; it < 8; it++) {
+    for (int k = 0; k < 3; k++) q[k] = std::fmaf(e, m[k], c[k]);
+    if ((side(P, q) > 0.0f) == front) return true;
+    e = e * 4.0f;
+  }
+  for (int k = 0; k < 3; k++) q[k] = c[k];
+  return false;
+}
+
+// the walk of one move; false = absorbed, x1 = where the molecule ends
+bool walk(const or_system* s, int sp, const float start[3], float x1[3]) {
+  float x0[3] = {start[0], start[1], start[2]};
+  for (int hit = 0; hit < 8; hit++) {
+    int best = -1;
+    float best_t = 2.0f;
+    bool best_front = false;
+    for (int id = 0; id < s->n_panels; id++) {
+      const or_panel& P = s->panels[id];
+      const uint8_t* act = s->surf_act + ((size_t)P.surface * s->S + sp) * 2;
+      if (act[0] == 0 && act[1] == 0) continue;
+      float t;
+      bool ff;
+      if (crossing(P, x0, x1, side(P, x0), side(P, x1), &t, &ff) && t < best_t) {
+        best = id;
+        best_t = t;
+        best_front = ff;
+      }
+    }
+    if (best < 0) return true;
+    const or_panel& P = s->panels[best];
+    const uint8_t action = s->surf_act[((size_t)P.surface * s->S + sp) * 2 + (best_front ? 0 : 1)];
+    if (action == 2) return false;
+    float c[3], q[3];
+    for (int k = 0; k < 3; k++) c[k] = std::fmaf(best_t, x1[k] - x0[k], x0[k]);
+    if (action == 0) {
+      onto_face(P, c, !best_front, q);
+    } else {
+      const bool start_on_face = (side(P, x0) > 0.0f) == best_front;
+      mirror(P, c, x1);
+      if (!onto_face(P, c, best_front, q) && start_on_face)
+        for (int k = 0; k < 3; k++) q[k] = x0[k];
+    }
+    for (int k = 0; k < 3; k++) x0[k] = q[k];
+  }
+  for (int k = 0; k < 3; k++) x1[k] = x0[k];
+  return true;
+}
+
+// the walls reflect first (the move's chord stays in the box, so a panel
+// that reaches a wall cannot be passed by way of the wall) and once more
+// after the walk, whose reflections can leave the box
+bool walk_in_box(const or_system* s, int sp, const float start[3], float x1[3]) {
+  if (!walk(s, sp, start, x1)) return false;
+  for (int a = 0; a < 3; a++) x1[a] = wall(x1[a], s->lo[a], s->hi[a]);
+  return true;
+}
+
 struct Model {
   const or_system* s;
   Rng rng;
@@ -202,7 +436,10 @@ int advance(const Model& m, uint32_t t, uint32_t i, const Rec& in, Rec out[2], u
     g[2] = rc * cosf(pc);
   }
   float p[3] = {in.x, in.y, in.z};
-  for (int a = 0; a < 3; a++) p[a] = wall(std::fmaf(m.sigma[sp], g[a], p[a]), s->lo[a], s->hi[a]);
+  float to[3];
+  for (int a = 0; a < 3; a++) to[a] = wall(std::fmaf(m.sigma[sp], g[a], p[a]), s->lo[a], s->hi[a]);
+  if (s->n_panels > 0 && !walk_in_box(s, sp, p, to)) return 0;  // absorbed
+  for (int a = 0; a < 3; a++) p[a] = to[a];
   int species = sp;
   int n = 1;
   const std::vector<int>& list = m.uni[sp];
@@ -219,16 +456,31 @@ int advance(const Model& m, uint32_t t, uint32_t i, const Rec& in, Rec out[2], u
       species = s->prod0[r];
       if (s->prod1[r] >= 0) {
         float b[3] = {p[0], p[1], p[2]};
+        bool alive0 = true, alive1 = true;
         if (s->off0[r] != 0.0f || s->off1[r] != 0.0f) {
-          float d[3];
+          float d[3], a0[3];
           direction(m.rng, i, t, T_UNIDIR, 0, d);
           for (int a = 0; a < 3; a++) {
             b[a] = wall(std::fmaf(s->off1[r], d[a], p[a]), s->lo[a], s->hi[a]);
-            p[a] = wall(std::fmaf(s->off0[r], d[a], p[a]), s->lo[a], s->hi[a]);
+            a0[a] = wall(std::fmaf(s->off0[r], d[a], p[a]), s->lo[a], s->hi[a]);
           }
+          if (s->n_panels > 0) {
+            alive1 = walk_in_box(s, s->prod1[r], p, b);
+            alive0 = walk_in_box(s, s->prod0[r], p, a0);
+          }
+          for (int a = 0; a < 3; a++) p[a] = a0[a];
         }
-        out[1] = Rec{b[0], b[1], b[2], pack(s->inst, s->prod1[r]) | NEWBORN};
-        n = 2;
+        const Rec born{b[0], b[1], b[2], pack(s->inst, s->prod1[r]) | NEWBORN};
+        if (!alive0) {
+          // the first product was absorbed on its way out: only the second is left
+          if (!alive1) return 0;
+          out[0] = born;
+          return 1;
+        }
+        if (alive1) {
+          out[1] = born;
+          n = 2;
+        }
       }
       break;
     }
@@ -437,15 +689,17 @@ extern "C" int or_step(const or_system* s, uint32_t t, const uint32_t* in, uint3
       float d[3] = {0.0f, 0.0f, 0.0f};
       if (s->off0[r] != 0.0f || s->off1[r] != 0.0f) direction(m.rng, q.i, t, T_BIMDIR, q.j, d);
       const Rec dead{0.0f, 0.0f, 0.0f, DEAD};
-      Rec n1 = dead, n2 = dead;
-      if (s->prod0[r] >= 0)
-        n1 = Rec{wall(std::fmaf(s->off0[r], d[0], rp[0]), s->lo[0], s->hi[0]),
-                 wall(std::fmaf(s->off0[r], d[1], rp[1]), s->lo[1], s->hi[1]),
-                 wall(std::fmaf(s->off0[r], d[2], rp[2]), s->lo[2], s->hi[2]), pack(s->inst, s->prod0[r])};
-      if (s->prod1[r] >= 0)
-        n2 = Rec{wall(std::fmaf(s->off1[r], d[0], rp[0]), s->lo[0], s->hi[0]),
-                 wall(std::fmaf(s->off1[r], d[1], rp[1]), s->lo[1], s->hi[1]),
-                 wall(std::fmaf(s->off1[r], d[2], rp[2]), s->lo[2], s->hi[2]), pack(s->inst, s->prod1[r])};
+      // a product moves from the reaction point by its offset (through the
+      // surfaces), then the walls reflect it
+      auto product = [&](int sp, float off) {
+        if (sp < 0) return dead;
+        float e[3];
+        for (int a = 0; a < 3; a++) e[a] = wall(std::fmaf(off, d[a], rp[a]), s->lo[a], s->hi[a]);
+        if (s->n_panels > 0 && off != 0.0f && !walk_in_box(s, sp, rp, e)) return dead;
+        return Rec{e[0], e[1], e[2], pack(s->inst, sp)};
+      };
+      const Rec n1 = product(s->prod0[r], s->off0[r]);
+      const Rec n2 = product(s->prod1[r], s->off1[r]);
       res[m1] = n1;
       res[m2] = n2;
       ev_total[r]++;

@@ -18,6 +18,20 @@
 extern "C" {
 #endif
 
+/* One surface panel with its derived geometry, word for word the library's
+ * bd_panel_info (shape 0 rect, 1 tri, 2 sphere, 3 cylinder, 4 hemisphere,
+ * 5 disk). */
+typedef struct or_panel {
+  int shape, surface, axis;
+  float front;
+  float a[3];
+  float r, r2;
+  float n[3];
+  float len;
+  float v1[3], v2[3];
+  float bounds[4];
+} or_panel;
+
 typedef struct or_system {
   float lo[3], hi[3], inv[3];
   float cell[3];
@@ -38,6 +52,9 @@ typedef struct or_system {
   int threads;              /* OpenMP threads, 0 = default */
   int channels;             /* 1: second-order reactions of one pair compete */
   const float *thresh;      /* per reaction: cumulative share of its pair's rate */
+  int n_panels;             /* surface panels (0 = none) */
+  const or_panel *panels;
+  const uint8_t *surf_act;  /* [surface][species][front, back]: 0 transmit, 1 reflect, 2 absorb */
 } or_system;
 
 /* One step.  in/out hold n records of 4 words (x, y, z as float bits, w).

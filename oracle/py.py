@@ -26,7 +26,8 @@ class or_system(C.Structure):
                 ("R", C.c_int), ("order", ip), ("react0", ip), ("react1", ip), ("prod0", ip), ("prod1", ip),
                 ("prob", fp), ("bind_radius", fp), ("off0", fp), ("off1", fp), ("cdf", dp), ("cdf_off", ip),
                 ("cdf_len", ip), ("cdf_kmin", ip), ("sorted", C.c_int), ("inst", C.c_uint32),
-                ("threads", C.c_int), ("channels", C.c_int), ("thresh", fp)]
+                ("threads", C.c_int), ("channels", C.c_int), ("thresh", fp), ("n_panels", C.c_int),
+                ("panels", C.c_void_p), ("surf_act", C.c_void_p)]
 
 
 _lib = None
@@ -59,6 +60,7 @@ class OracleSystem:
     """Oracle inputs for one instance of a library handle."""
 
     def __init__(self, sys, instance=0, threads=0, sorted_path=None):
+        from gpusmoldyn_gb300 import _lib as L
         from gpusmoldyn_gb300.system import gauss_table
 
         self.keep = []
@@ -115,9 +117,27 @@ class OracleSystem:
         for name in ("prob", "bind_radius", "off0", "off1", "thresh", "D", "gauss"):
             setattr(s, name, arrs[name].ctypes.data_as(fp))
         s.cdf = arrs["cdf"].ctypes.data_as(dp)
+        # surfaces: the panels' derived geometry (bd_panel_info words) and the
+        # [surface][species][front, back] action table, read through the C ABI
+        n_surf, n_pan = sys.surface_counts()
+        pan = np.zeros((max(n_pan, 1), 23), np.uint32)
+        for k in range(n_pan):
+            q = L.bd_panel_info()
+            L.check(sys.lib.bd_get_panel(sys.h, k, C.byref(q)), "bd_get_panel")
+            pan[k] = np.frombuffer(bytes(q), np.uint32)
+        act = np.zeros(max(n_surf * sys.n_species * 2, 1), np.uint8)
+        for f in range(n_surf):
+            for sp in range(sys.n_species):
+                for face in (0, 1):
+                    act[(f * sys.n_species + sp) * 2 + face] = sys.surface_action(f, sp, face)
+        arrs["panels"] = pan
+        arrs["surf_act"] = act
+        s.n_panels = n_pan
+        s.panels = pan.ctypes.data
+        s.surf_act = act.ctypes.data
         if sorted_path is None:
             sorted_path = (sys.n_instances > 1 or any(i["order"] in (1, 2) for i in info)
-                           or any(i["order"] == 0 and i["nprod"] == 2 for i in info))
+                           or any(i["order"] == 0 and i["nprod"] == 2 for i in info) or n_pan > 0)
         s.sorted = 1 if sorted_path else 0
         s.inst = instance
         s.threads = threads

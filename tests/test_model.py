@@ -122,3 +122,70 @@ def test_model_file(tmp_path):
     assert info["n_molecules"] == 36000
     with pytest.raises(L.BDError, match="cannot read"):
         System.from_model(path=tmp_path / "missing.txt", device=None)
+
+
+SURF_MODEL = """
+dim 3
+boundaries x 0 10
+boundaries y 0 10
+boundaries z 0 10
+species A B
+difc all 1
+time_step 0.001
+max_surface 3
+start_surface membrane
+  action all both reflect
+  action B front absorb
+  color both 0.5 0.5 0.5     # display: ignored
+  panel sph 5 5 5 3 20 20 ball
+end_surface
+start_surface walls
+  action front all transmit
+  action back A reflect
+  panel rect +x 8 0 0 10 10
+  panel rect -2 0 0 9.5 10 10
+  panel tri 1 1 1 2 1 1 1 2 1
+  panel cyl 2 2 2 2 2 8 -1 12 12
+  panel hemi 7 7 7 1 0 0 1 10 10
+  panel disk 3 3 3 0.5 0 1 0
+end_surface
+surface walls action A both absorb
+mol 100 A u u u
+"""
+
+
+def test_model_surfaces():
+    m, info = System.from_model(SURF_MODEL, device=None)
+    assert m.surface_counts() == (2, 7)
+    A, B = m.species_id("A"), m.species_id("B")
+    assert m.surface_action(0, A, "front") == L.BD_SURF_REFLECT
+    assert [m.surface_action(0, B, f) for f in ("front", "back")] == [L.BD_SURF_ABSORB, L.BD_SURF_REFLECT]
+    assert [m.surface_action(1, A, f) for f in ("front", "back")] == [L.BD_SURF_ABSORB] * 2
+    assert [m.surface_action(1, B, f) for f in ("front", "back")] == [L.BD_SURF_TRANSMIT] * 2
+    p = [m.panel_info(k) for k in range(7)]
+    assert [q["shape"] for q in p] == [L.BD_PANEL_SPH, L.BD_PANEL_RECT, L.BD_PANEL_RECT, L.BD_PANEL_TRI,
+                                       L.BD_PANEL_CYL, L.BD_PANEL_HEMI, L.BD_PANEL_DISK]
+    assert p[0]["r"] == 3 and p[0]["front"] == 1.0
+    assert (p[1]["axis"], p[1]["front"], p[1]["bounds"]) == (0, 1.0, [0, 10, 0, 10])
+    assert (p[2]["axis"], p[2]["front"], p[2]["a"]) == (2, -1.0, [0, 0, 9.5])
+    assert p[4]["front"] == -1.0 and p[4]["r"] == 1 and p[4]["len"] == 6
+    assert [q["surface"] for q in p] == [0, 1, 1, 1, 1, 1, 1]
+
+
+@pytest.mark.parametrize("bad, code, where", [
+    ("start_surface s\n  action all both jump\nend_surface", L.BD_ERR_UNSUPPORTED, "line 8"),
+    ("start_surface s\n  rate A fsoln bsoln 1\nend_surface", L.BD_ERR_UNSUPPORTED, "line 8"),
+    ("start_surface s\n  panel rect x 0 0 0 1 1\nend_surface", L.BD_ERR_INVALID_ARGUMENT, "line 8"),
+    ("start_surface s\n  panel sph 1 1 1\nend_surface", L.BD_ERR_INVALID_ARGUMENT, "needs 4"),
+    ("start_surface s\n  panel tri 0 0 0 1 1 1 2 2 2\nend_surface", L.BD_ERR_INVALID_ARGUMENT, "degenerate"),
+    ("start_surface s\n  panel box 0 0 0 1\nend_surface", L.BD_ERR_UNSUPPORTED, "box"),
+    ("start_surface s\n  action Q both reflect\nend_surface", L.BD_ERR_INVALID_ARGUMENT, "unknown species Q"),
+    ("start_surface s\n  panel sph 1 1 1 1", L.BD_ERR_INVALID_ARGUMENT, "without end_surface"),
+])
+def test_malformed_surfaces_name_the_line(bad, code, where):
+    text = "species A B C\n" + bad.replace("start_surface", "\n".join(
+        ["boundaries 0 0 20", "boundaries 1 0 20", "boundaries 2 0 20", "time_step 0.001", "difc all 1",
+         "start_surface"]))
+    with pytest.raises(L.BDError) as e:
+        System.from_model(text, device=None)
+    assert e.value.code == code and where in str(e.value)
