@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-surfaces", action="store_true")
     p.add_argument("--serve-jobs", type=int, default=40)
     p.add_argument("--profile-only", action="store_true", help="build + a few steps (for ncu)")
     return p.parse_args()
@@ -379,6 +380,10 @@ def run_gb300(args, dist):
                       "path": "bd_set_particles + steps x (bd_step(1) + bd_get_count) + bd_get_particles"}
         s3.close()
 
+    # ---------------- the same step with surfaces (c3 inside a cell)
+    if not args.no_surfaces and args.workload == "c3":
+        out["surfaces"] = run_surfaces(args, dist, device, out["value"])
+
     # ---------------- batched ensemble vs the plain per-instance loop
     if not args.no_batched:
         out["batched"] = run_batched(args, dist, device)
@@ -395,6 +400,30 @@ def run_gb300(args, dist):
                                "sample": f"c3 network at the c3 density: 262144 particles in a {side:.1f} um cube,"
                                          f" {done} steps ({el:.1f} s), OpenMP {threads} threads"}
     return out
+
+
+def run_surfaces(args, dist, device, plain_value):
+    """The c3 step inside a cell: a spherical membrane (one sphere panel) and
+    a nucleus of 1280 triangles, walked by every diffusion step."""
+    from gpusmoldyn_gb300 import configs
+
+    n = args.n or 16_000_000
+    side = 200.0 * (n / 16_000_000) ** (1 / 3)
+    s = configs.build_c3(n=n, side=side, surfaces=True, device=device)
+    s.step(args.warmup)
+    s.synchronize()
+    steps = max(args.steps // 4, 20)
+    n0 = s.count()
+    ms = s.time_steps(steps)
+    n1 = s.count()
+    value = dist.sum(steps * 0.5 * (n0 + n1)) / (dist.max(ms) / 1e3)
+    prof = s.profile_steps(10)
+    n_surf, n_panels = s.surface_counts()
+    s.close()
+    return {"workload": f"c3 inside a cell: {n} particles, {n_panels} panels in {n_surf} surfaces "
+                        "(reflecting membrane crossed by S0 and S1, nucleus of 1280 triangles)",
+            "value": value, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
+            "vs_plain_step": value / plain_value, "kernel_ms_per_step": {k: v / 10 for k, v in prof.items()}}
 
 
 def run_batched(args, dist, device):

@@ -181,10 +181,50 @@ def c3_add_network(s, density, network_seed=3):
     return frac
 
 
-def c3_system(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
-    """The c3 network in a `side` cube, finalized, without particles."""
+def icosphere(centre, radius, levels):
+    """Triangles (k, 3, 3) of an icosahedron subdivided `levels` times and
+    pushed onto the sphere, vertices counterclockwise seen from outside."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    V = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    tris = np.array([[V[a], V[b], V[c]] for a, b, c in F], np.float64)
+    tris /= np.linalg.norm(tris, axis=2, keepdims=True)
+    for _ in range(levels):
+        a, b, c = tris[:, 0], tris[:, 1], tris[:, 2]
+        ab, bc, ca = (a + b) / 2, (b + c) / 2, (c + a) / 2
+        tris = np.concatenate([np.stack(q, 1) for q in ((a, ab, ca), (ab, b, bc), (ca, bc, c), (ab, bc, ca))])
+        tris /= np.linalg.norm(tris, axis=2, keepdims=True)
+    return np.asarray(centre, np.float64) + radius * tris
+
+
+def c3_cell_surfaces(s, side):
+    """The c3 network inside a cell: a spherical membrane (radius 0.4 side)
+    that reflects every species but the two small ligands S0 and S1, which
+    cross it, and a nucleus (radius 0.12 side, an icosphere of 1280
+    triangles) that reflects every species.  Nothing is absorbed, so the
+    stationary composition of the plain c3 run is kept."""
+    c = (side / 2, side / 2, side / 2)
+    membrane = s.add_surface()
+    s.set_surface_action(membrane, -1, "both", "reflect")
+    for lig in (0, 1):
+        s.set_surface_action(membrane, lig, "both", "transmit")
+    s.add_panel(membrane, "sph", [c[0], c[1], c[2], 0.4 * side])
+    nucleus = s.add_surface()
+    s.set_surface_action(nucleus, -1, "both", "reflect")
+    for tri in icosphere(c, 0.12 * side, 3):
+        s.add_panel(nucleus, "tri", list(tri.ravel()))
+
+
+def c3_system(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, surfaces=False, **kw):
+    """The c3 network in a `side` cube, finalized, without particles
+    (surfaces: inside the cell of c3_cell_surfaces)."""
     s = System((0, 0, 0), (side, side, side), dt=1e-3, seed=seed, normals=normals, **kw)
     c3_add_network(s, n / side ** 3, network_seed)
+    if surfaces:
+        c3_cell_surfaces(s, side)
     s.finalize()
     return s
 
@@ -198,8 +238,8 @@ def c3_particles(n=16_000_000, side=200.0, seed=3, network_seed=3):
     return pos, c3_species(n, frac)
 
 
-def build_c3(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, **kw):
-    s = c3_system(n, side, seed, normals, network_seed, **kw)
+def build_c3(n=16_000_000, side=200.0, seed=3, normals="boxmuller", network_seed=3, surfaces=False, **kw):
+    s = c3_system(n, side, seed, normals, network_seed, surfaces, **kw)
     s.set_particles(*c3_particles(n, side, seed, network_seed))
     return s
 

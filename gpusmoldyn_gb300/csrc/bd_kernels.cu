@@ -642,14 +642,16 @@ __device__ __forceinline__ void emit(const KParams& p, DevCtrl* c, const Seeker&
             inst_of<kSingle>(p, k.inst));
 }
 
-// Pairs of record k (canonical slot ca, in `cell`) with the records of the
-// 13 forward neighbour cells (higher key) whose shared face, edge or corner
-// lies within its largest binding radius.  Every cross-cell pair within
-// range is found from its lower-key side only, so each is tested once.
-// The record's cell coordinates are recomputed from its position exactly
-// as the sort computed its key (cell_coord), which avoids integer division.
-template <bool kBinned, bool kSingle>
-__device__ __forceinline__ void search_forward(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t ca) {
+// The forward neighbour cells (higher key) of record k that its largest
+// binding radius reaches: the cells whose shared face, edge or corner lies
+// within it.  Every cross-cell pair within range is found from its
+// lower-key side only, so each is tested once.  Bit b of the result names
+// neighbour b: 0 = (+1, 0, 0); 1..3 = (-1..+1, +1, 0); 4..12 = (-1..+1,
+// -1..+1, +1) in (dx, dy, dz), dx fastest.  *key0 receives the record's own
+// cell key.  The cell coordinates are recomputed from the position exactly
+// as the sort computed the key (cell_coord), which avoids integer division.
+template <bool kSingle>
+__device__ __forceinline__ uint32_t forward_mask(const KParams& p, const Seeker& k, uint32_t* key0) {
   const DevInstance& I = inst_of<kSingle>(p, k.inst);
   const float cl0 = I.cell[0], cl1 = I.cell[1], cl2 = I.cell[2];
   const uint32_t d0 = I.dims[0], d1 = I.dims[1], d2 = I.dims[2];
@@ -659,6 +661,7 @@ __device__ __forceinline__ void search_forward(const KParams& p, DevCtrl* c, con
   const int cx = min(max((int)floorf(gx), 0), (int)d0 - 1);
   const int cy = min(max((int)floorf(gy), 0), (int)d1 - 1);
   const int cz = min(max((int)floorf(gz), 0), (int)d2 - 1);
+  *key0 = I.cell_base + ((uint32_t)cz * d1 + (uint32_t)cy) * d0 + (uint32_t)cx;
   const float margin = p.prune_margin * fminf(cl0, fminf(cl1, cl2));
   const float need = k.max_r + margin;
   const float fx = __fsub_rn(gx, (float)cx), fy = __fsub_rn(gy, (float)cy), fz = __fsub_rn(gz, (float)cz);
@@ -667,12 +670,12 @@ __device__ __forceinline__ void search_forward(const KParams& p, DevCtrl* c, con
   const int zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
   const int yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
   const int xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
-  if ((zhi | yhi | xhi) == 0) return;
+  if ((zhi | yhi | xhi) == 0) return 0u;
   const float lox = fx * cl0, loy = fy * cl1;
   const float need2 = need * need;
   const int ylo = (cy > 0 && loy <= need) ? -1 : 0;
   const int xlo = (cx > 0 && lox <= need) ? -1 : 0;
-  const uint32_t cbase = I.cell_base;
+  uint32_t mask = 0;
   for (int dz = 0; dz <= zhi; ++dz) {
     const float ddz = dz > 0 ? hiz : 0.0f;
     for (int dy = (dz > 0 ? ylo : 0); dy <= yhi; ++dy) {
@@ -680,17 +683,42 @@ __device__ __forceinline__ void search_forward(const KParams& p, DevCtrl* c, con
       for (int dx = (dz > 0 || dy > 0 ? xlo : 1); dx <= xhi; ++dx) {
         const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
         if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
-        const uint32_t nkey = cbase + ((uint32_t)(cz + dz) * d1 + (uint32_t)(cy + dy)) * d0 + (uint32_t)(cx + dx);
-        const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
-        if (nn > kBigCell) continue;  // pairs with large cells are found by k_pairs_big_pairs
-        const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
-        for (uint32_t m = 0; m < nn; ++m) {
-          const float4 q = __ldg(&nb[m]);
-          const int32_t b = pair_reaction(p, k, q);
-          if (b >= 0) emit<kSingle>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
-        }
+        const int b = dz > 0 ? 4 + (dy + 1) * 3 + (dx + 1) : (dy > 0 ? 2 + dx : 0);
+        mask |= 1u << b;
       }
     }
+  }
+  return mask;
+}
+
+// Key of forward neighbour b (bit numbering of forward_mask) of cell key0.
+__device__ __forceinline__ uint32_t forward_key(uint32_t key0, uint32_t b, uint32_t d0, uint32_t d1) {
+  int dx, dy, dz;
+  if (b == 0) {
+    dx = 1, dy = 0, dz = 0;
+  } else if (b < 4) {
+    dx = (int)b - 2, dy = 1, dz = 0;
+  } else {
+    const int q = (int)b - 4;
+    dx = q % 3 - 1, dy = q / 3 - 1, dz = 1;
+  }
+  return (uint32_t)((int)key0 + (dz * (int)d1 + dy) * (int)d0 + dx);
+}
+
+// Pairs of record r (canonical slot ca) with the records of neighbour cell
+// nkey, found from r's side.
+template <bool kBinned, bool kSingle>
+__device__ __forceinline__ void visit_neighbour(const KParams& p, DevCtrl* c, const float4& r, uint32_t ca,
+                                                uint32_t nkey) {
+  Seeker k;
+  if (!seeker_init<kSingle>(p, r, k)) return;
+  const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
+  if (nn > kBigCell) return;  // pairs with large cells are found by k_pairs_big_pairs
+  const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
+  for (uint32_t m = 0; m < nn; ++m) {
+    const float4 q = __ldg(&nb[m]);
+    const int32_t b = pair_reaction(p, k, q);
+    if (b >= 0) emit<kSingle>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
   }
 }
 
@@ -705,14 +733,45 @@ __device__ __forceinline__ void search_forward(const KParams& p, DevCtrl* c, con
 //   * in the same loop marks the cell's later records (storage order)
 //     whose x lies within its largest binding radius; only those are read
 //     in full and tested, each in-cell pair once;
-//   * searches the forward neighbour cells (search_forward).
+//   * marks the forward neighbour cells its binding radius reaches
+//     (forward_mask) and queues one visit per cell in the warp's shared
+//     queue; the warp visits them 32 at a time, one per lane, so the few
+//     records near a face do not hold the whole warp through a visit's
+//     chain of dependent loads (cell start, records, tables).
 // Canonical slots of partners are computed only for pairs within range.
 // Cells above kBigCell records are queued for the large-cell kernels.  kBinned: the
 // records come from the cell bins, whose counts are cleared here for the
 // next step; otherwise from the compact scatter buffer.
+constexpr uint32_t kVisitQueue = 64;  // queued visits per warp (< 32 between drains, + one round's push)
+
+// Visits queued by a warp: the visit of queue entry `lane`.
+struct VisitQueue {
+  float4 rec[kVisitQueue];
+  uint32_t ca[kVisitQueue], key[kVisitQueue];
+};
+
+// Visit the first 32 queued entries, one per lane, and move the rest
+// (vq - 32 < 32 entries) to the front.  Warp-uniform call.
+template <bool kBinned, bool kSingle>
+__device__ __forceinline__ void drain_visits(const KParams& p, DevCtrl* c, VisitQueue& q, uint32_t vq) {
+  const uint32_t lane = lane_id();
+  __syncwarp();
+  const float4 r = q.rec[lane];
+  const uint32_t ca = q.ca[lane], key = q.key[lane];
+  __syncwarp();
+  if (lane + 32u < vq) {
+    q.rec[lane] = q.rec[lane + 32u];
+    q.ca[lane] = q.ca[lane + 32u];
+    q.key[lane] = q.key[lane + 32u];
+  }
+  __syncwarp();
+  visit_neighbour<kBinned, kSingle>(p, c, r, ca, key);
+}
+
 template <bool kHasBim, bool kBinned, bool kSingle>
 __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   __shared__ uint32_t s_cell[8][32], s_cs[8][32], s_n[8][32], s_off[8][32];
+  __shared__ VisitQueue s_visit[kHasBim ? 8 : 1];
   DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
   const uint32_t cur = ld_u32(&c->cur);
@@ -721,6 +780,8 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   const uint32_t n_tasks = (p.n_cells + 31u) >> 5;
   const uint32_t nw = gridDim.x * (blockDim.x >> 5);
   const uint32_t le_mask = lane == 31 ? kFull : ((2u << lane) - 1u);
+  VisitQueue& vqueue = s_visit[kHasBim ? warp : 0];
+  uint32_t vq = 0;  // queued visits (warp-uniform)
   // Cells are taken from the highest key down: the bins written last by
   // k_bin (its records stream in ascending cell order) are still in L2,
   // and the next state's low slots, written last here, are the first the
@@ -759,12 +820,14 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
     for (uint32_t rb = 0; rb < total; rb += 32u) {
       const uint32_t M = __reduce_or_sync(kFull, (n > 0 && off >= rb && off - rb < 32u) ? 1u << (off - rb) : 0u);
       const uint32_t t = rb + lane;
+      uint32_t nbm = 0, key0 = 0, ca = 0;  // forward cells to visit from this lane's record
+      float4 ra = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (t < total) {
         const uint32_t oq = before + __popc(M & le_mask) - 1u;
         const uint32_t ocell = s_cell[warp][oq], ocs = s_cs[warp][oq], on = s_n[warp][oq];
         const uint32_t j = t - s_off[warp][oq];
         const float4* __restrict__ cb = cell_records<kBinned>(p, ocell, ocs);
-        const float4 ra = __ldg(&cb[j]);
+        ra = __ldg(&cb[j]);
         Seeker k;
         const bool search = kHasBim && seeker_init<kSingle>(p, ra, k);
         const float xlim = search ? k.xlim : -1.0f;
@@ -780,7 +843,7 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
           if (m > j && m < 32u && fabsf(__fsub_rn(qx, ra.x)) <= xlim) cand |= 1u << m;
         }
         if (tie) rank = canonical_rank(cb, 0, on, j, ra);
-        const uint32_t ca = ocs + rank;
+        ca = ocs + rank;
         if (ca < p.capacity) nx[ca] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
         else atomicOr(&c->status, kStatBounds);
         if (search) {
@@ -796,12 +859,40 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
             const int32_t bb = pair_reaction(p, k, qm);
             if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
           }
-          search_forward<kBinned, kSingle>(p, c, k, ca);
+          nbm = forward_mask<kSingle>(p, k, &key0);
+        }
+      }
+      if (kHasBim) {
+        // queue one visit per marked neighbour cell, draining 32 at a time
+        const DevInstance& I = inst_of<kSingle>(p, kSingle ? 0u : rec_w(ra) >> 16);
+        while (__any_sync(kFull, nbm != 0u)) {
+          const bool has = nbm != 0u;
+          uint32_t nkey = 0;
+          if (has) {
+            nkey = forward_key(key0, (uint32_t)(__ffs(nbm) - 1), I.dims[0], I.dims[1]);
+            nbm &= nbm - 1u;
+          }
+          const uint32_t ball = __ballot_sync(kFull, has);
+          if (has) {
+            const uint32_t pos = vq + __popc(ball & ((1u << lane) - 1u));
+            vqueue.rec[pos] = ra;
+            vqueue.ca[pos] = ca;
+            vqueue.key[pos] = nkey;
+          }
+          vq += __popc(ball);
+          if (vq >= 32u) {
+            drain_visits<kBinned, kSingle>(p, c, vqueue, vq);
+            vq -= 32u;
+          }
         }
       }
       before += __popc(M);
     }
     __syncwarp();
+  }
+  if (kHasBim) {
+    __syncwarp();
+    if (lane < vq) visit_neighbour<kBinned, kSingle>(p, c, vqueue.rec[lane], vqueue.ca[lane], vqueue.key[lane]);
   }
 }
 
