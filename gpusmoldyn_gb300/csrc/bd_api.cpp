@@ -93,6 +93,9 @@ struct bd_system {
   DevBuf<DevPanel> dpanels;
   DevBuf<uint8_t> dsurf_act;
   DevBuf<uint32_t> dpbox_start, dpbox_list;
+  DevBuf<uint32_t> surf_queue;  // [capacity] when there are panels
+  DevBuf<uint8_t> dcell_surf;    // [n_cells] species masks of the cells near panels
+  std::vector<uint8_t> panel_species;  // per panel: species_bit of every species whose step may meet it
   PanelGrid pgrid{};
 
   // device
@@ -204,6 +207,8 @@ KParams make_params(bd_system* h) {
     p.surf_act = h->dsurf_act.p;
     p.pbox_start = h->dpbox_start.p;
     p.pbox_list = h->dpbox_list.p;
+    p.surf_queue = h->surf_queue.p;
+    p.cell_surf = h->dcell_surf.p;
     for (int k = 0; k < 3; k++) {
       p.pbox_lo[k] = h->pgrid.lo[k];
       p.pbox_inv[k] = h->pgrid.inv[k];
@@ -376,6 +381,7 @@ bd_status grow_particles(bd_system* h, uint64_t cap) {
   if (!h->binned) BD_CUDA(sc.alloc(cap));
   BD_CUDA(best.alloc(cap));
   BD_CUDA(cudaMemsetAsync(best.p, 0xFF, cap * sizeof(uint32_t), h->stream));
+  if (!h->panels.empty()) BD_CUDA(h->surf_queue.alloc(cap));
   // cells above 128 records (the large-cell kernel's queue) number at most cap / 129
   BD_CUDA(h->big.alloc(cap / 129 + 2));
   if (h->big_scratch.n) BD_CUDA(h->big_scratch.alloc(cap));
@@ -435,6 +441,8 @@ void plan_instance(bd_system* h, int k, uint64_t n) {
   D.flags = kInstActive;
 }
 
+bd_status upload_cell_masks(bd_system* h);
+
 // Consecutive cell ranges for the instances in instance order (unused
 // server slots get a single cell), the cell arrays and the instance table.
 bd_status layout_cells(bd_system* h) {
@@ -466,6 +474,10 @@ bd_status layout_cells(bd_system* h) {
   BD_CUDA(cudaMemsetAsync(h->cell_start.p, 0, ((size_t)h->n_cells + 1) * sizeof(uint32_t), h->stream));
   BD_CUDA(h->tile_sums.alloc(std::max<uint32_t>(h->n_tiles, 1)));
   BD_CUDA(cudaStreamSynchronize(h->stream));
+  if (!h->panels.empty()) {
+    const bd_status st = upload_cell_masks(h);
+    if (st) return st;
+  }
   // Bins hold the planned occupancy of the densest instance with room for
   // Poisson fluctuations (mean + 7 sd + 8: an overflow at mean 3 has
   // probability ~1e-14 per cell and step); they only grow.
@@ -608,6 +620,8 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->dsurf_act.free();
   h->dpbox_start.free();
   h->dpbox_list.free();
+  h->surf_queue.free();
+  h->dcell_surf.free();
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return BD_OK;
@@ -692,6 +706,48 @@ void plan_panel_grid(bd_system* h) {
       hi[k] = std::max(hi[k], d.box_hi[k]);
     }
   build_panel_grid(h->panels, lo, hi, &h->pgrid);
+  // a step of species s walks s and the products of its first-order
+  // reactions: the panel counts for s when any of them sees it
+  const int S = (int)h->D.size();
+  std::vector<std::vector<int>> walked(S);
+  for (int sp = 0; sp < S; sp++) walked[sp].push_back(sp);
+  for (const ReactionDef& r : h->rx)
+    if (r.order == 1)
+      for (int k = 0; k < 2; k++)
+        if (r.products[k] >= 0) walked[r.reactants[0]].push_back(r.products[k]);
+  h->panel_species.assign(h->panels.size(), 0);
+  for (size_t id = 0; id < h->panels.size(); id++)
+    for (int sp = 0; sp < S; sp++)
+      for (int t : walked[sp])
+        if (surface_action(h, h->panels[id].surface, t, 0) != kActTransmit ||
+            surface_action(h, h->panels[id].surface, t, 1) != kActTransmit)
+          h->panel_species[id] |= (uint8_t)(1u << species_bit(sp));
+}
+
+// Species masks of every cell (build_cell_masks), instance by instance,
+// looked up at the cell a step starts in.  The reach of an instance bounds
+// how far a molecule's diffusion step goes (Box-Muller and table normals
+// stay within 5.9 sigma per axis) plus the largest first-order product
+// offset from the step's end.
+bd_status upload_cell_masks(bd_system* h) {
+  std::vector<uint8_t> m(h->n_cells, 0xFF);
+  for (int k = 0; k < h->n_inst(); k++) {
+    if (h->server && !h->slot_used[k]) continue;  // a single cell, nothing moves there
+    const DevInstance& D = h->hinst[k];
+    const DerivedParams& P = h->derived[k];
+    double smax = 0.0, omax = 0.0;
+    for (float sg : P.sigma) smax = std::max(smax, (double)sg);
+    for (int r = 0; r < h->R; r++)
+      if (h->rx[r].order == 1) omax = std::max({omax, (double)fabsf(P.rx[r].off[0]), (double)fabsf(P.rx[r].off[1])});
+    double box = 0.0;
+    for (int a = 0; a < 3; a++) box = std::max({box, (double)fabsf(D.lo[a]), (double)fabsf(D.hi[a])});
+    const double reach = (6.0 * smax + omax) * 1.001 + 1e-5 * (box + 1.0);
+    build_cell_masks(h->panels, h->panel_species, h->pgrid, D.lo, D.cell, D.dims, reach, &m[D.cell_base]);
+  }
+  BD_CUDA(h->dcell_surf.alloc(std::max<size_t>(m.size(), 1)));
+  BD_CUDA(cudaMemcpyAsync(h->dcell_surf.p, m.data(), m.size(), cudaMemcpyHostToDevice, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  return BD_OK;
 }
 
 bd_status pack_blocks(bd_system* h) {
@@ -1075,6 +1131,7 @@ BD_API bd_status bd_synchronize(bd_handle h) {
       c.status = 0;
       c.n_pairs = 0;
       c.n_big = 0;
+      c.n_surf = 0;
       c.n_virtual = 0;
       st = push_ctrl(h);
       if (st) return st;
@@ -1573,7 +1630,7 @@ BD_API const char* bd_stage_name(bd_handle h, int k) {
 BD_API bd_status bd_get_kernels_per_step(bd_handle h, int* n) {
   if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
   if (h->diffuse_only()) *n = (h->Z > 0 ? 2 : 0) + 2;
-  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 7 : 8) + (h->B > 0 ? 1 : 0);
+  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 7 : 8) + (h->B > 0 ? 1 : 0) + (h->binned && !h->panels.empty() ? 1 : 0);
   return BD_OK;
 }
 

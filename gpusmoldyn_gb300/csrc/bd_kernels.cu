@@ -165,9 +165,14 @@ __device__ __forceinline__ bool surface_walk(const KParams& p, const DevInstance
   return true;
 }
 
-// kSurf walks each displacement (the diffusion step, product offsets)
-// through the surface panels.
-template <bool kTable, bool kCount, bool kSingle, bool kSurf = false>
+// kSurf = 1 walks each displacement (the diffusion step, product offsets)
+// through the surface panels.  kSurf = 2 looks up the species mask of the
+// cell where the step starts (cell_surf): a set bit means a panel the
+// species sees lies within reach of the step or of the products it may
+// place, and the record stops after its diffusion with o.n = -1 so that
+// the caller queues it for a walk (k_bin_surface); other records finish
+// here, and no panel could have changed their step.
+template <bool kTable, bool kCount, bool kSingle, int kSurf = 0>
 __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& ctx, const float4 rec, uint32_t i,
                                             Out2& o) {
   o.n = 0;
@@ -187,6 +192,9 @@ __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& c
   const uint32_t t = kSingle ? ctx.step : p.inst_step[inst];
   const uint32_t k0 = I.key_lo, k1 = I.key_hi;
   const DevSpecies S = kSingle ? ctx.species[sp] : p.species[I.block * p.S + sp];
+  // the species mask of the cell the step starts in, loaded before the
+  // arithmetic that hides its latency
+  const uint32_t near = kSurf == 2 ? __ldg(&p.cell_surf[cell_key(I, rec.x, rec.y, rec.z)]) : 0u;
 
   const U4 rn = philox(U4{local, t, kTagDiffuse, 0u}, k0, k1);
   float g0, g1, g2;
@@ -194,7 +202,11 @@ __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& c
   float x = reflect(__fmaf_rn(S.sigma, g0, rec.x), I.lo[0], I.hi[0]);
   float y = reflect(__fmaf_rn(S.sigma, g1, rec.y), I.lo[1], I.hi[1]);
   float z = reflect(__fmaf_rn(S.sigma, g2, rec.z), I.lo[2], I.hi[2]);
-  if (kSurf && !surface_walk(p, I, sp, V3{rec.x, rec.y, rec.z}, x, y, z)) return;  // absorbed
+  if (kSurf == 2 && ((near >> (sp < 7u ? sp : 7u)) & 1u)) {
+    o.n = -1;
+    return;
+  }
+  if (kSurf == 1 && !surface_walk(p, I, sp, V3{rec.x, rec.y, rec.z}, x, y, z)) return;  // absorbed
   uint32_t species = sp;
   int n = 1;
 
@@ -220,14 +232,14 @@ __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& c
           x = reflect(__fmaf_rn(u.off0, dx, x), I.lo[0], I.hi[0]);
           y = reflect(__fmaf_rn(u.off0, dy, y), I.lo[1], I.hi[1]);
           z = reflect(__fmaf_rn(u.off0, dz, z), I.lo[2], I.hi[2]);
-          if (kSurf) {
+          if (kSurf == 1) {
             // both products move from the reaction point
             keep1 = surface_walk(p, I, (uint32_t)u.prod1, from, bx, by, bz);
             keep0 = surface_walk(p, I, (uint32_t)u.prod0, from, x, y, z);
           }
         }
         const float4 born = make_float4(bx, by, bz, __uint_as_float(pack_w(inst, (uint32_t)u.prod1) | kNewborn));
-        if (kSurf && !keep0) {  // the first product was absorbed: the birth takes its place
+        if (kSurf == 1 && !keep0) {  // the first product was absorbed: the birth takes its place
           if (!keep1) return;
           o.r[0] = born;
           o.key[0] = cell_key(I, bx, by, bz);
@@ -236,7 +248,7 @@ __device__ __forceinline__ void advance_rec(const KParams& p, const SingleCtx& c
         }
         o.r[1] = born;
         o.key[1] = cell_key(I, bx, by, bz);
-        n = (kSurf && !keep1) ? 1 : 2;
+        n = (kSurf == 1 && !keep1) ? 1 : 2;
       }
       break;
     }
@@ -372,7 +384,7 @@ __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
 
 // kMinBlocks 4 / 6 cap registers at 64 / 40 (50% / 75% occupancy, the
 // latter with a few spills); the launch shape picks the variant.
-template <bool kTable, int kMinBlocks, bool kSingle, bool kSurf = false>
+template <bool kTable, int kMinBlocks, bool kSingle, int kSurf = 0>
 __global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
   __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
@@ -449,7 +461,7 @@ __global__ void __launch_bounds__(1024) k_scan_down(KParams p) {
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) p.cell_start[p.n_cells] = ld_u32(&c->n_sorted);
 }
 
-template <bool kTable, int kMinBlocks, bool kSingle, bool kSurf = false>
+template <bool kTable, int kMinBlocks, bool kSingle, int kSurf = 0>
 __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
   __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
@@ -520,10 +532,33 @@ __device__ __forceinline__ void claim_retire(const KParams& p, DevCtrl* c, const
 // the step's arithmetic runs once and nothing is recomputed.  First
 // products keep the deferred claim above; the rare second products (births)
 // claim and store at once.
-template <bool kTable, int kMinBlocks, bool kSingle, bool kSurf = false>
+// Slots a warp queues for k_bin_surface, written out 32 at a time with one
+// atomicAdd on the queue count (a record per lane and atomic would all meet
+// on that one word).
+struct DeferBuffer {
+  uint32_t slot[64];
+};
+
+__device__ __forceinline__ void defer_flush(const KParams& p, DevCtrl* c, DeferBuffer& b, uint32_t n) {
+  __syncwarp();
+  uint32_t base = 0;
+  if (lane_id() == 0) base = atomicAdd(&c->n_surf, n);
+  base = __shfl_sync(kFull, base, 0);
+  if (lane_id() < n) {
+    const uint32_t e = base + lane_id();
+    if (e < p.capacity) p.surf_queue[e] = b.slot[lane_id()];
+    else atomicOr(&c->status, kStatBounds);
+  }
+  __syncwarp();
+}
+
+template <bool kTable, int kMinBlocks, bool kSingle, int kSurf = 0>
 __global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
   __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
+  __shared__ DeferBuffer s_defer[kSurf == 2 ? 8 : 1];  // one per warp (blocks of at most 256 threads)
+  DeferBuffer& defer_buf = s_defer[kSurf == 2 ? threadIdx.x >> 5 : 0];
+  uint32_t n_defer = 0;  // slots in defer_buf (warp-uniform)
   SingleCtx ctx{};
   if (kSingle) ctx = single_ctx(p, s_species, s_uni);
   DevCtrl* c = p.ctrl;
@@ -541,12 +576,58 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
     o.n = 0;
     if (i < n_real) advance_rec<kTable, true, kSingle, kSurf>(p, ctx, rec, i, o);
     else if (i < n_total) advance_virtual<kSingle>(p, i - n_real, o);
+    if (kSurf == 2) {
+      // records near a panel go to k_bin_surface
+      const bool defer = o.n < 0;
+      const uint32_t ball = __ballot_sync(kFull, defer);
+      if (ball) {
+        if (defer) {
+          defer_buf.slot[n_defer + __popc(ball & ((1u << lane_id()) - 1u))] = i;
+          o.n = 0;
+        }
+        n_defer += __popc(ball);
+        if (n_defer >= 32u) {
+          defer_flush(p, c, defer_buf, 32u);
+          if (lane_id() + 32u < n_defer) defer_buf.slot[lane_id()] = defer_buf.slot[lane_id() + 32u];
+          __syncwarp();
+          n_defer -= 32u;
+        }
+      }
+    }
     const PendingClaim next = claim_issue(p.cell_count, o.n > 0 ? o.key[0] : kNoKey, o.r[0]);
     if (__any_sync(kFull, o.n > 1)) claim_retire(p, c, claim_issue(p.cell_count, o.n > 1 ? o.key[1] : kNoKey, o.r[1]));
     claim_retire(p, c, pending);
     pending = next;
   });
   claim_retire(p, c, pending);
+  if (kSurf == 2 && n_defer > 0) defer_flush(p, c, defer_buf, n_defer);
+}
+
+// Binned path with surfaces, pass 1b: the records k_bin queued because
+// their move meets a panel box, advanced with the surface walk (the same
+// Philox counters, so the same step) and put into their bins.
+template <bool kTable, bool kSingle>
+__global__ void __launch_bounds__(256, 2) k_bin_surface(KParams p) {
+  __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
+  __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
+  SingleCtx ctx{};
+  if (kSingle) ctx = single_ctx(p, s_species, s_uni);
+  DevCtrl* c = p.ctrl;
+  if (ctrl_status_warp(c)) return;
+  const float4* __restrict__ st = cur_state(p, ld_u32(&c->cur));
+  const uint32_t n = min(ld_u32(&c->n_surf), p.capacity);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {  // CTA-uniform trip count
+    const uint32_t e = base + threadIdx.x;
+    Out2 o;
+    o.n = 0;
+    if (e < n) {
+      const uint32_t i = p.surf_queue[e];
+      advance_rec<kTable, true, kSingle, 1>(p, ctx, st[i], i, o);
+    }
+    claim_retire(p, c, claim_issue(p.cell_count, o.n > 0 ? o.key[0] : kNoKey, o.r[0]));
+    if (__any_sync(kFull, o.n > 1)) claim_retire(p, c, claim_issue(p.cell_count, o.n > 1 ? o.key[1] : kNoKey, o.r[1]));
+  }
 }
 
 // Position of record r among the records of its cell [s, e) in canonical
@@ -1269,6 +1350,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     c->n_pairs_last = K;
     c->n_pairs = 0;
     c->n_big = 0;
+    c->n_surf = 0;
     c->deaths_last = s_deaths;
     c->n_slots = c->n_sorted;
     c->n_virtual = 0;
@@ -1389,38 +1471,31 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   }
   // Register-capped variants of the streaming kernels, picked by the launch
   // shape's resident CTAs per SM: 1 = no cap, 4 = 64 registers, 6 = 40.
-#define BD_STREAM_LAUNCH3(KERNEL, MINB)                                                    \
+#define BD_STREAM_LAUNCH3(KERNEL, MINB, SURF)                                              \
   do {                                                                                     \
     if (single) {                                                                          \
-      if (table) KERNEL<true, MINB, true><<<gs, bs, 0, s>>>(p);                             \
-      else KERNEL<false, MINB, true><<<gs, bs, 0, s>>>(p);                                  \
+      if (table) KERNEL<true, MINB, true, SURF><<<gs, bs, 0, s>>>(p);                       \
+      else KERNEL<false, MINB, true, SURF><<<gs, bs, 0, s>>>(p);                            \
     } else {                                                                               \
-      if (table) KERNEL<true, MINB, false><<<gs, bs, 0, s>>>(p);                            \
-      else KERNEL<false, MINB, false><<<gs, bs, 0, s>>>(p);                                 \
+      if (table) KERNEL<true, MINB, false, SURF><<<gs, bs, 0, s>>>(p);                      \
+      else KERNEL<false, MINB, false, SURF><<<gs, bs, 0, s>>>(p);                           \
     }                                                                                      \
   } while (0)
   // With surfaces: one variant per kernel, no register cap.
-#define BD_STREAM_LAUNCH_SURF(KERNEL)                                                      \
-  do {                                                                                     \
-    if (single) {                                                                          \
-      if (table) KERNEL<true, 1, true, true><<<gs, bs, 0, s>>>(p);                          \
-      else KERNEL<false, 1, true, true><<<gs, bs, 0, s>>>(p);                               \
-    } else {                                                                               \
-      if (table) KERNEL<true, 1, false, true><<<gs, bs, 0, s>>>(p);                         \
-      else KERNEL<false, 1, false, true><<<gs, bs, 0, s>>>(p);                              \
-    }                                                                                      \
+#define BD_STREAM_LAUNCH(KERNEL, SURF)                   \
+  do {                                                   \
+    switch (shape.min_blocks) {                          \
+      case 6: BD_STREAM_LAUNCH3(KERNEL, 6, SURF); break; \
+      case 4: BD_STREAM_LAUNCH3(KERNEL, 4, SURF); break; \
+      default: BD_STREAM_LAUNCH3(KERNEL, 1, SURF);       \
+    }                                                    \
   } while (0)
-#define BD_STREAM_LAUNCH(KERNEL)                     \
-  do {                                               \
-    if (p.n_panels) {                                \
-      BD_STREAM_LAUNCH_SURF(KERNEL);                 \
-    } else {                                         \
-      switch (shape.min_blocks) {                    \
-        case 6: BD_STREAM_LAUNCH3(KERNEL, 6); break; \
-        case 4: BD_STREAM_LAUNCH3(KERNEL, 4); break; \
-        default: BD_STREAM_LAUNCH3(KERNEL, 1);       \
-      }                                              \
-    }                                                \
+  // The compact path walks the surfaces inline: one variant per kernel, no
+  // register cap.
+#define BD_STREAM_LAUNCH_COMPACT(KERNEL)          \
+  do {                                            \
+    if (p.n_panels) BD_STREAM_LAUNCH3(KERNEL, 1, 1); \
+    else BD_STREAM_LAUNCH(KERNEL, 0);             \
   } while (0)
 #define BD_PAIRS_LAUNCH(BINNED)                                                                      \
   do {                                                                                               \
@@ -1434,8 +1509,21 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   } while (0)
   const bool single = p.n_inst == 1 && p.S <= kCtxSpecies && p.U <= kCtxUni;
   if (path == Path::kBinned) {
-    BD_STREAM_LAUNCH(k_bin);
-    done("k_bin");
+    if (p.n_panels) {
+      BD_STREAM_LAUNCH(k_bin, 2);
+      done("k_bin");
+      if (single) {
+        if (table) k_bin_surface<true, true><<<gs, bs, 0, s>>>(p);
+        else k_bin_surface<false, true><<<gs, bs, 0, s>>>(p);
+      } else {
+        if (table) k_bin_surface<true, false><<<gs, bs, 0, s>>>(p);
+        else k_bin_surface<false, false><<<gs, bs, 0, s>>>(p);
+      }
+      done("k_bin_surface");
+    } else {
+      BD_STREAM_LAUNCH(k_bin, 0);
+      done("k_bin");
+    }
     k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
     done("k_scan_tiles");
     k_scan_top<<<1, 1024, 0, s>>>(p);
@@ -1455,7 +1543,7 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     done("k_match");
     return n;
   }
-  BD_STREAM_LAUNCH(k_count);
+  BD_STREAM_LAUNCH_COMPACT(k_count);
   done("k_count");
   k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
   done("k_scan_tiles");
@@ -1463,11 +1551,11 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   done("k_scan_top");
   k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
   done("k_scan_down");
-  BD_STREAM_LAUNCH(k_scatter);
+  BD_STREAM_LAUNCH_COMPACT(k_scatter);
   done("k_scatter");
   BD_PAIRS_LAUNCH(false);
 #undef BD_STREAM_LAUNCH
-#undef BD_STREAM_LAUNCH_SURF
+#undef BD_STREAM_LAUNCH_COMPACT
 #undef BD_STREAM_LAUNCH3
 #undef BD_PAIRS_LAUNCH
   done("k_pairs_cells");

@@ -50,6 +50,8 @@ struct KParams {
   float pbox_lo[3], pbox_inv[3];
   uint32_t pbox_dims[3];
   uint32_t n_panels;
+  uint32_t* surf_queue;       // [capacity] slots whose move may meet a panel (k_bin -> k_bin_surface)
+  const uint8_t* cell_surf;   // [n_cells] species masks: a step starting here may meet a panel (species_bit)
 };
 
 // kSorted: counting sort into compact cell ranges (k_count, scans,

@@ -110,7 +110,8 @@ struct DevCtrl {
   uint32_t deaths_last;    // bimolecular deaths of the last step
   uint32_t bin_need;       // largest cell occupancy seen by a bin that overflowed
   uint32_t n_big;          // cells queued for the large-cell pair kernel
-  uint32_t pad[3];
+  uint32_t n_surf;         // records whose move meets a panel box (binned path with surfaces)
+  uint32_t pad[2];
 };
 
 enum StatusBits : uint32_t {

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <thread>
 
 namespace bd {
 
@@ -144,6 +145,57 @@ void panel_aabb(const bd_panel_info& P, double lo[3], double hi[3]) {
   }
 }
 
+// False when the panel cannot pass through the box [lo, hi] grown by pad:
+// a sphere or hemisphere whose surface misses it (box inside, or wholly
+// outside, the sphere), a cylinder that contains the box, a triangle whose
+// plane leaves every corner on one side.  Panels are kept in doubt.
+bool panel_meets_box(const bd_panel_info& P, const double lo[3], const double hi[3], double pad) {
+  double c[8][3];
+  for (int k = 0; k < 8; k++)
+    for (int a = 0; a < 3; a++) c[k][a] = ((k >> a) & 1) ? hi[a] + pad : lo[a] - pad;
+  switch (P.shape) {
+    case BD_PANEL_SPH:
+    case BD_PANEL_HEMI: {
+      double near2 = 0.0, far2 = 0.0;
+      for (int a = 0; a < 3; a++) {
+        const double l = lo[a] - pad - P.a[a], h = hi[a] + pad - P.a[a];
+        const double n = l > 0 ? l : (h < 0 ? -h : 0.0);
+        near2 += n * n;
+        far2 += std::max(l * l, h * h);
+      }
+      const double r = P.r;
+      return near2 <= r * r && far2 >= r * r;
+    }
+    case BD_PANEL_CYL: {
+      for (int k = 0; k < 8; k++) {
+        double w[3], t = 0.0, q = 0.0;
+        for (int a = 0; a < 3; a++) {
+          w[a] = c[k][a] - P.a[a];
+          t += w[a] * P.n[a];
+        }
+        for (int a = 0; a < 3; a++) {
+          const double d = w[a] - t * P.n[a];
+          q += d * d;
+        }
+        if (q >= (double)P.r * P.r) return true;  // a corner outside the infinite cylinder
+      }
+      return false;
+    }
+    case BD_PANEL_TRI: {
+      bool pos = false, neg = false;
+      for (int k = 0; k < 8; k++) {
+        double s = 0.0;
+        for (int a = 0; a < 3; a++) s += (c[k][a] - P.a[a]) * P.n[a];
+        pos |= s >= 0.0;
+        neg |= s <= 0.0;
+      }
+      return pos && neg;
+    }
+    default:
+      return true;
+  }
+}
+
 }  // namespace
 
 void build_panel_grid(const std::vector<bd_panel_info>& panels, const float lo[3], const float hi[3], PanelGrid* g) {
@@ -166,17 +218,28 @@ void build_panel_grid(const std::vector<bd_panel_info>& panels, const float lo[3
     double a[3], b[3];
     panel_aabb(panels[id], a, b);
     int r0[3], r1[3];
+    double edge[3], pad_all = 0.0;
     for (int k = 0; k < 3; k++) {
-      const double edge = ext[k] / g->dims[k];
-      const double pad = 1e-3 * edge + 1e-6 * (std::fabs(a[k]) + std::fabs(b[k]) + 1.0);
-      const double f0 = std::floor((a[k] - pad - lo[k]) / edge), f1 = std::floor((b[k] + pad - lo[k]) / edge);
+      edge[k] = ext[k] / g->dims[k];
+      const double pad = 1e-3 * edge[k] + 1e-6 * (std::fabs(a[k]) + std::fabs(b[k]) + 1.0);
+      pad_all = std::max(pad_all, pad);
+      const double f0 = std::floor((a[k] - pad - lo[k]) / edge[k]), f1 = std::floor((b[k] + pad - lo[k]) / edge[k]);
       r0[k] = (int)std::min<double>(std::max<double>(f0, 0.0), g->dims[k] - 1.0);
       r1[k] = (int)std::min<double>(std::max<double>(f1, 0.0), g->dims[k] - 1.0);
     }
     for (int z = r0[2]; z <= r1[2]; z++)
       for (int y = r0[1]; y <= r1[1]; y++)
-        for (int x = r0[0]; x <= r1[0]; x++)
+        for (int x = r0[0]; x <= r1[0]; x++) {
+          // the edge boxes take every position beyond the grid as well
+          const int i3[3] = {x, y, z};
+          double blo[3], bhi[3];
+          for (int k = 0; k < 3; k++) {
+            blo[k] = i3[k] == 0 ? -1e30 : lo[k] + i3[k] * edge[k];
+            bhi[k] = i3[k] == (int)g->dims[k] - 1 ? 1e30 : lo[k] + (i3[k] + 1) * edge[k];
+          }
+          if (!panel_meets_box(panels[id], blo, bhi, pad_all)) continue;
           boxes[((uint32_t)z * g->dims[1] + (uint32_t)y) * g->dims[0] + (uint32_t)x].push_back((uint32_t)id);
+        }
   }
   g->start.assign(nb + 1, 0);
   g->list.clear();
@@ -185,6 +248,54 @@ void build_panel_grid(const std::vector<bd_panel_info>& panels, const float lo[3
     g->list.insert(g->list.end(), boxes[b].begin(), boxes[b].end());
   }
   g->start[nb] = (uint32_t)g->list.size();
+}
+
+void build_cell_masks(const std::vector<bd_panel_info>& panels, const std::vector<uint8_t>& panel_species,
+                      const PanelGrid& g, const float lo[3], const float cell[3], const uint32_t dims[3],
+                      double reach, uint8_t* out) {
+  std::vector<double> plo(panels.size() * 3), phi(panels.size() * 3);
+  for (size_t id = 0; id < panels.size(); id++) panel_aabb(panels[id], &plo[3 * id], &phi[3 * id]);
+  double pedge[3];
+  for (int k = 0; k < 3; k++) pedge[k] = 1.0 / g.inv[k];
+  const double pad = 1e-4 * std::min({(double)cell[0], (double)cell[1], (double)cell[2]}) +
+                     1e-6 * (std::fabs(lo[0]) + std::fabs(lo[1]) + std::fabs(lo[2]) + 1.0);
+  auto slab = [&](uint32_t z0, uint32_t z1) {
+    for (uint32_t z = z0; z < z1; z++)
+      for (uint32_t y = 0; y < dims[1]; y++)
+        for (uint32_t x = 0; x < dims[0]; x++) {
+          const uint32_t c3[3] = {x, y, z};
+          double blo[3], bhi[3];
+          int r0[3], r1[3];
+          for (int k = 0; k < 3; k++) {
+            blo[k] = (double)lo[k] + (double)c3[k] * cell[k] - reach;
+            bhi[k] = (double)lo[k] + (double)(c3[k] + 1) * cell[k] + reach;
+            const double f0 = std::floor((blo[k] - pad - g.lo[k]) / pedge[k]);
+            const double f1 = std::floor((bhi[k] + pad - g.lo[k]) / pedge[k]);
+            r0[k] = (int)std::min<double>(std::max<double>(f0, 0.0), g.dims[k] - 1.0);
+            r1[k] = (int)std::min<double>(std::max<double>(f1, 0.0), g.dims[k] - 1.0);
+          }
+          uint8_t m = 0;
+          for (int bz = r0[2]; bz <= r1[2] && m != 0xFF; bz++)
+            for (int by = r0[1]; by <= r1[1] && m != 0xFF; by++)
+              for (int bx = r0[0]; bx <= r1[0] && m != 0xFF; bx++) {
+                const uint32_t box = ((uint32_t)bz * g.dims[1] + (uint32_t)by) * g.dims[0] + (uint32_t)bx;
+                for (uint32_t e = g.start[box]; e < g.start[box + 1]; e++) {
+                  const uint32_t id = g.list[e];
+                  if (!(panel_species[id] & ~m)) continue;
+                  bool apart = false;
+                  for (int k = 0; k < 3; k++)
+                    apart |= plo[3 * id + k] > bhi[k] + pad || phi[3 * id + k] < blo[k] - pad;
+                  if (!apart && panel_meets_box(panels[id], blo, bhi, pad)) m |= panel_species[id];
+                }
+              }
+          out[((size_t)z * dims[1] + y) * dims[0] + x] = m;
+        }
+  };
+  const uint32_t nt = std::max(1u, std::min<uint32_t>(std::thread::hardware_concurrency(), dims[2]));
+  std::vector<std::thread> pool;
+  for (uint32_t t = 0; t < nt; t++)
+    pool.emplace_back(slab, (uint32_t)((uint64_t)dims[2] * t / nt), (uint32_t)((uint64_t)dims[2] * (t + 1) / nt));
+  for (std::thread& th : pool) th.join();
 }
 
 }  // namespace bd
