@@ -361,23 +361,30 @@ def run_gb300(args, dist):
     # ---------------- end to end through the C ABI with host buffers
     if not args.no_e2e:
         s3, pos, sp = network_and_particles(args.workload, args.n, device)
+        # the caller's arrays in the reference's layout: float4 positions, int species
+        pos4 = np.zeros((len(sp), 4), np.float32)
+        pos4[:, :3] = pos
+        sp = np.ascontiguousarray(sp, np.int32)
         dist.barrier()
         t0 = time.perf_counter()
-        s3.set_particles(pos, sp)
+        s3.set_particles(pos4, sp)
+        ta = time.perf_counter()
         psteps = 0
         live = len(sp)
         for _ in range(args.steps):
             s3.step(1)
             live = s3.count()
             psteps += live
-        pos_out, sp_out = s3.particles()
+        tb = time.perf_counter()
+        pos_out, sp_out = s3.particles4()
         t1 = time.perf_counter()
         dist.barrier()
         e2e_s = dist.max(t1 - t0)
         out["e2e"] = {"value": dist.sum(psteps) / e2e_s, "unit": UNIT,
                       "h2d_bytes_per_step": 20 * len(sp) / args.steps,
                       "d2h_bytes_per_step": 8 + 20 * len(sp_out) / args.steps,
-                      "path": "bd_set_particles + steps x (bd_step(1) + bd_get_count) + bd_get_particles"}
+                      "path": "bd_set_particles + steps x (bd_step(1) + bd_get_count) + bd_get_particles",
+                      "seconds": {"set_particles": ta - t0, "steps": tb - ta, "get_particles": t1 - tb}}
         s3.close()
 
     # ---------------- the same step with surfaces (c3 inside a cell)

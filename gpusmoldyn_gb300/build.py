@@ -17,8 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgpusmoldyn.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["bd_kernels.cu", "bd_static_sort.cu", "bd_api.cpp", "bd_params.cpp", "bd_model.cpp", "bd_output.cpp",
-           "bd_surface.cpp", "particle_system.cpp"]
+SOURCES = ["bd_kernels.cu", "bd_static_sort.cu", "bd_io.cu", "bd_api.cpp", "bd_params.cpp", "bd_model.cpp",
+           "bd_output.cpp", "bd_surface.cpp", "particle_system.cpp"]
 
 
 def nvcc() -> str:

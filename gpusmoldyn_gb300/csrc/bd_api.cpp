@@ -15,10 +15,12 @@
 #include <string.h>
 
 #include <algorithm>
+#include <initializer_list>
 #include <string>
 #include <vector>
 
 #include "../../include/gpusmoldyn.h"
+#include "bd_io.h"
 #include "bd_kernels.h"
 #include "bd_layout.h"
 #include "bd_params.h"
@@ -496,30 +498,88 @@ bd_status layout_cells(bd_system* h) {
   return ensure_sort_buffers(h, K);
 }
 
+// Device scratch of one call, taken from the stream-ordered pool and given
+// back on the stream when the call returns.
+struct Scratch {
+  cudaStream_t stream = nullptr;
+  char* p = nullptr;
+  size_t used = 0;
+  ~Scratch() {
+    if (p) cudaFreeAsync(p, stream);
+  }
+  cudaError_t alloc(size_t bytes, cudaStream_t s) {
+    stream = s;
+    return cudaMallocAsync((void**)&p, bytes, s);
+  }
+  template <class T>
+  T* take(size_t count) {  // 256-byte aligned pieces
+    T* q = reinterpret_cast<T*>(p + used);
+    used += (count * sizeof(T) + 255) & ~(size_t)255;
+    return q;
+  }
+};
+
+size_t scratch_bytes(std::initializer_list<size_t> sizes) {
+  size_t b = 0;
+  for (size_t x : sizes) b += (x + 255) & ~(size_t)255;
+  return b;
+}
+
+// The caller's particles (float4 x, y, z, w and int species, counts[k] for
+// instance k in instance order) become the current state.  On a device
+// handle they are copied whole to device scratch, checked there (species
+// range, inside the instance's box) before anything of the handle changes,
+// and packed into records by a kernel.
 bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, const uint64_t* counts) {
   if (!h->finalized) return BD_ERR_NOT_FINALIZED;
   const int I = h->n_inst();
   uint64_t n = 0;
   for (int k = 0; k < I; k++) n += counts[k];
   if (n > 0 && (!xyz4 || !species)) return BD_ERR_INVALID_ARGUMENT;
-  std::vector<float4> recs(n);
   std::vector<uint32_t> slot_base(I, 0);
-  uint64_t i = 0;
+  std::vector<uint64_t> start(I + 1, 0);
+  std::vector<float> boxes(6 * (size_t)I);
   for (int k = 0; k < I; k++) {
-    slot_base[k] = (uint32_t)i;
-    const bd_instance_desc& d = h->idesc[k];
-    for (uint64_t j = 0; j < counts[k]; j++, i++) {
-      const int s = species[i];
-      if (s < 0 || s >= h->S) return BD_ERR_INVALID_ARGUMENT;
-      float x = xyz4[4 * i], y = xyz4[4 * i + 1], z = xyz4[4 * i + 2];
-      if (!(x >= d.box_lo[0] && x <= d.box_hi[0] && y >= d.box_lo[1] && y <= d.box_hi[1] && z >= d.box_lo[2] &&
-            z <= d.box_hi[2]))
-        return BD_ERR_INVALID_ARGUMENT;
-      uint32_t w = ((uint32_t)k << 16) | (uint32_t)s;
-      float wf;
-      memcpy(&wf, &w, 4);
-      recs[i] = make_float4(x, y, z, wf);
+    start[k + 1] = start[k] + counts[k];
+    slot_base[k] = (uint32_t)start[k];
+    for (int a = 0; a < 3; a++) {
+      boxes[6 * k + a] = h->idesc[k].box_lo[a];
+      boxes[6 * k + 3 + a] = h->idesc[k].box_hi[a];
     }
+  }
+  Scratch scratch;
+  UploadArgs up{};
+  if (h->host_only) {
+    for (int k = 0; k < I; k++)
+      for (uint64_t i = start[k]; i < start[k + 1]; i++) {
+        const int s = species[i];
+        const float x = xyz4[4 * i], y = xyz4[4 * i + 1], z = xyz4[4 * i + 2];
+        const float* b = &boxes[6 * k];
+        if (s < 0 || s >= h->S || !(x >= b[0] && x <= b[3] && y >= b[1] && y <= b[4] && z >= b[2] && z <= b[5]))
+          return BD_ERR_INVALID_ARGUMENT;
+      }
+  } else if (n > 0) {
+    BD_CUDA(cudaSetDevice(h->device));
+    BD_CUDA(scratch.alloc(scratch_bytes({n * sizeof(float4), n * sizeof(int), (I + 1) * sizeof(uint64_t),
+                                         boxes.size() * sizeof(float), sizeof(uint32_t)}),
+                          h->stream));
+    float4* d_xyz4 = scratch.take<float4>(n);
+    int* d_species = scratch.take<int>(n);
+    uint64_t* d_start = scratch.take<uint64_t>(I + 1);
+    float* d_boxes = scratch.take<float>(boxes.size());
+    uint32_t* d_bad = scratch.take<uint32_t>(1);
+    BD_CUDA(cudaMemcpyAsync(d_xyz4, xyz4, n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemcpyAsync(d_species, species, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemcpyAsync(d_start, start.data(), (I + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemcpyAsync(d_boxes, boxes.data(), boxes.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(uint32_t), h->stream));
+    up = UploadArgs{d_xyz4, d_species, d_start, d_boxes, n, I, h->S, d_bad};
+    enqueue_upload_check(up, h->stream);
+    BD_CUDA(cudaGetLastError());
+    uint32_t bad = 0;
+    BD_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    BD_CUDA(cudaStreamSynchronize(h->stream));
+    if (bad) return BD_ERR_INVALID_ARGUMENT;
   }
   h->hinst.assign(I, DevInstance{});
   for (int k = 0; k < I; k++) plan_instance(h, k, counts[k]);
@@ -530,12 +590,25 @@ bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, 
   if (cap < n) cap = n;
   h->have_particles = false;
   memset(h->hctrl, 0, sizeof(DevCtrl));
-  st = grow_particles(h, cap);
-  if (st) return st;
+  // buffers of the same size are kept (the matcher scratch is all ones
+  // again after every step)
+  const bool same = cap == h->capacity && h->state0.p && h->state1.p && (h->binned || h->scatter.n >= cap) &&
+                    (h->panels.empty() || h->surf_queue.n >= cap);
+  if (same) {
+    h->hctrl->cur = 0;
+  } else {
+    st = grow_particles(h, cap);
+    if (st) return st;
+  }
   uint32_t pc = h->cfg.pair_capacity ? h->cfg.pair_capacity : (uint32_t)std::max<uint64_t>(65536, cap / 32);
-  st = grow_pairs(h, pc);
-  if (st) return st;
-  if (n) BD_CUDA(cudaMemcpyAsync(h->state0.p, recs.data(), n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  if (pc != h->pair_cap || !h->pairs.p) {
+    st = grow_pairs(h, pc);
+    if (st) return st;
+  }
+  if (n) {
+    enqueue_upload_pack(up, h->state0.p, h->stream);
+    BD_CUDA(cudaGetLastError());
+  }
   std::vector<uint32_t> zeros(I, 0);
   st = upload(h->inst_step, zeros, h->stream);
   if (st) return st;
@@ -1192,27 +1265,34 @@ BD_API bd_status bd_get_instance_particles(bd_handle h, int inst, float* xyz4, i
   if (inst >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
   *n = 0;
   if (!h->have_particles) return BD_OK;
-  std::vector<float4> slots;
-  bd_status st = read_slots(h, &slots);
-  if (st) return st;
-  size_t k = 0;
-  for (const float4& r : slots) {
-    uint32_t w;
-    memcpy(&w, &r.w, 4);
-    if (w == kDead) continue;
-    if (inst >= 0 && (int)(w >> 16) != inst) continue;
-    if (k < cap) {
-      if (xyz4) {
-        xyz4[4 * k] = r.x;
-        xyz4[4 * k + 1] = r.y;
-        xyz4[4 * k + 2] = r.z;
-        xyz4[4 * k + 3] = 1.0f;
-      }
-      if (species) species[k] = (int)(w & 0xFFFFu);
-    }
-    k++;
-  }
-  *n = k;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  // the live records in slot order, exported on the device and copied whole
+  const uint64_t slots = h->hctrl->n_slots;
+  const uint32_t tiles = export_tiles(slots);
+  Scratch scratch;
+  BD_CUDA(scratch.alloc(scratch_bytes({slots * sizeof(float4), slots * sizeof(int), tiles * sizeof(uint32_t),
+                                       sizeof(uint32_t)}),
+                        h->stream));
+  ExportArgs a{};
+  a.state = h->hctrl->cur ? h->state1.p : h->state0.p;
+  a.n_slots = slots;
+  a.inst = inst;
+  a.n_tiles = tiles;
+  a.xyz4 = scratch.take<float4>(slots);
+  a.species = scratch.take<int>(slots);
+  a.tile_offset = scratch.take<uint32_t>(tiles);
+  a.count = scratch.take<uint32_t>(1);
+  enqueue_export(a, h->stream);
+  BD_CUDA(cudaGetLastError());
+  uint32_t total = 0;
+  BD_CUDA(cudaMemcpyAsync(&total, a.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  const size_t m = std::min<size_t>(total, cap);
+  if (m && xyz4) BD_CUDA(cudaMemcpyAsync(xyz4, a.xyz4, m * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
+  if (m && species) BD_CUDA(cudaMemcpyAsync(species, a.species, m * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  *n = total;
   return BD_OK;
 }
 

@@ -219,10 +219,16 @@ class System:
 
     # ---------------------------------------------------------- particles
     def set_particles(self, pos, species):
+        """pos: (n, 3) or (n, 4) positions (a contiguous float32 (n, 4) array,
+        the reference's float4 layout, is passed without a copy)."""
         pos = np.asarray(pos, np.float32)
         n = pos.shape[0]
-        p4 = np.zeros((n, 4), np.float32)
-        p4[:, :3] = pos[:, :3]
+        if pos.ndim == 2 and pos.shape[1] == 4 and pos.flags.c_contiguous:
+            p4 = pos
+        else:
+            p4 = np.empty((n, 4), np.float32)
+            p4[:, :3] = pos[:, :3]
+            p4[:, 3] = 0.0
         sp = np.ascontiguousarray(species, np.int32)
         L.check(self.lib.bd_set_particles(self.h, _ptr(p4), _ptr(sp), n), "bd_set_particles")
 
@@ -259,15 +265,21 @@ class System:
         L.check(self.lib.bd_get_step(self.h, C.byref(v)), "bd_get_step")
         return v.value
 
-    def particles(self, instance=-1):
+    def particles4(self, instance=-1):
+        """Live particles in slot order as the reference's layout: (n, 4)
+        float32 positions (w = 1) and int32 species."""
         n = self.count() if instance < 0 else int(self.instance_counts()[instance])
-        pos = np.zeros((max(n, 1), 4), np.float32)
-        sp = np.zeros(max(n, 1), np.int32)
+        pos = np.empty((max(n, 1), 4), np.float32)
+        sp = np.empty(max(n, 1), np.int32)
         got = C.c_size_t()
         L.check(self.lib.bd_get_instance_particles(self.h, instance, _ptr(pos), _ptr(sp), n, C.byref(got)),
                 "bd_get_particles")
         m = min(got.value, n)
-        return pos[:m, :3].copy(), sp[:m].copy()
+        return pos[:m], sp[:m]
+
+    def particles(self, instance=-1):
+        pos, sp = self.particles4(instance)
+        return np.ascontiguousarray(pos[:, :3]), sp
 
     def species_counts(self, instance=-1) -> np.ndarray:
         out = np.zeros(max(self.n_species, 1), np.uint64)
