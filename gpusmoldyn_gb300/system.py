@@ -265,12 +265,21 @@ class System:
         L.check(self.lib.bd_get_step(self.h, C.byref(v)), "bd_get_step")
         return v.value
 
-    def particles4(self, instance=-1):
+    def particles4(self, instance=-1, out=None):
         """Live particles in slot order as the reference's layout: (n, 4)
-        float32 positions (w = 1) and int32 species."""
+        float32 positions (w = 1) and int32 species.  out = (pos, species)
+        arrays the caller keeps between calls (contiguous float32 (cap, 4)
+        and int32 (cap,)) are filled instead of new ones; the views returned
+        hold the first n."""
         n = self.count() if instance < 0 else int(self.instance_counts()[instance])
-        pos = np.empty((max(n, 1), 4), np.float32)
-        sp = np.empty(max(n, 1), np.int32)
+        if out is not None:
+            pos, sp = out
+            if (pos.dtype != np.float32 or sp.dtype != np.int32 or pos.ndim != 2 or pos.shape[1] != 4
+                    or not pos.flags.c_contiguous or not sp.flags.c_contiguous or len(pos) < n or len(sp) < n):
+                raise ValueError("out: contiguous float32 (>= n, 4) and int32 (>= n,) arrays")
+        else:
+            pos = np.empty((max(n, 1), 4), np.float32)
+            sp = np.empty(max(n, 1), np.int32)
         got = C.c_size_t()
         L.check(self.lib.bd_get_instance_particles(self.h, instance, _ptr(pos), _ptr(sp), n, C.byref(got)),
                 "bd_get_particles")
