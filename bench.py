@@ -478,13 +478,19 @@ def run_serving(args, device):
     from gpusmoldyn_gb300 import configs
     from gpusmoldyn_gb300.serve import Server
 
+    from gpusmoldyn_gb300.serve import c3_request
+
     jobs = configs.c5_jobs(args.serve_jobs, seed=5)
+    # each request arrives with its initial state (the client builds it)
+    for j in jobs:
+        j["payload"] = c3_request(j)
     srv = Server(max_instances=64, hbm_budget=150e9, chunk=10, device=device)
     res = srv.run(jobs)
     srv.close()
     return {"workload": f"c5: {len(jobs)} requests, Poisson 50/s, N log-U[1e3, 5e6], steps U[100, 10000]",
             "p50_latency_s": res["p50_s"], "p99_latency_s": res["p99_s"], "mean_latency_s": res["mean_s"],
-            "value": res["particle_steps_per_s"], "unit": UNIT, "wall_s": res["wall_s"], "jobs": res["jobs"]}
+            "value": res["particle_steps_per_s"], "unit": UNIT, "wall_s": res["wall_s"], "jobs": res["jobs"],
+            "seconds": {k: round(v, 4) for k, v in res["host_seconds"].items()}}
 
 
 def main():

@@ -142,7 +142,7 @@ struct bd_system {
   std::vector<uint8_t> slot_used;        // admitted, not yet harvested
   std::vector<uint64_t> slot_free_after; // removed: free once ctrl.step exceeds this
   std::vector<uint32_t> h_flags, h_target;
-  DevBuf<uint32_t> inst_flags, inst_target;
+  DevBuf<uint32_t> inst_flags, inst_target, inst_frozen;
 
   bool diffuse_only() const {
     return U == 0 && B == 0 && idesc.size() == 1 && !zero_two_products && !server && panels.empty();
@@ -183,6 +183,7 @@ KParams make_params(bd_system* h) {
   p.inst_step = h->inst_step.p;
   p.inst_flags = h->inst_flags.p;
   p.inst_target = h->inst_target.p;
+  p.inst_frozen = h->inst_frozen.p;
   p.inst_slot_base = h->inst_slot_base.p;
   p.zero_off = h->zero_off.p;
   p.cell_count = h->cell_count.p;
@@ -468,13 +469,16 @@ bd_status layout_cells(bd_system* h) {
   h->n_cells = (uint32_t)base;
   h->n_tiles = (uint32_t)((base + kScanTile - 1) / kScanTile);
   if (h->host_only) return BD_OK;
-  BD_CUDA(h->dinst.alloc(I));
+  // grow-only: a serving handle lays its cells out again at every admission,
+  // and cudaFree would wait for the whole device
+  auto ensure = [](auto& buf, size_t count) { return buf.p && buf.n >= count ? cudaSuccess : buf.alloc(count); };
+  BD_CUDA(ensure(h->dinst, (size_t)I));
   BD_CUDA(cudaMemcpyAsync(h->dinst.p, h->hinst.data(), I * sizeof(DevInstance), cudaMemcpyHostToDevice, h->stream));
-  BD_CUDA(h->cell_count.alloc(h->n_cells));
+  BD_CUDA(ensure(h->cell_count, (size_t)h->n_cells));
   BD_CUDA(cudaMemsetAsync(h->cell_count.p, 0, (size_t)h->n_cells * sizeof(uint32_t), h->stream));
-  BD_CUDA(h->cell_start.alloc((size_t)h->n_cells + 1));
+  BD_CUDA(ensure(h->cell_start, (size_t)h->n_cells + 1));
   BD_CUDA(cudaMemsetAsync(h->cell_start.p, 0, ((size_t)h->n_cells + 1) * sizeof(uint32_t), h->stream));
-  BD_CUDA(h->tile_sums.alloc(std::max<uint32_t>(h->n_tiles, 1)));
+  BD_CUDA(ensure(h->tile_sums, (size_t)std::max<uint32_t>(h->n_tiles, 1)));
   BD_CUDA(cudaStreamSynchronize(h->stream));
   if (!h->panels.empty()) {
     const bd_status st = upload_cell_masks(h);
@@ -616,7 +620,8 @@ bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, 
   if (st) return st;
   h->h_flags.assign(I, kInstActive);
   h->h_target.assign(I, 0xFFFFFFFFu);
-  if ((st = upload(h->inst_flags, h->h_flags, h->stream)) || (st = upload(h->inst_target, h->h_target, h->stream)))
+  if ((st = upload(h->inst_flags, h->h_flags, h->stream)) || (st = upload(h->inst_target, h->h_target, h->stream)) ||
+      (st = upload(h->inst_frozen, zeros, h->stream)))
     return st;
   BD_CUDA(h->zero_off.alloc((size_t)I * h->Z + 1));
   BD_CUDA(cudaMemsetAsync(h->zero_off.p, 0, ((size_t)I * h->Z + 1) * sizeof(uint32_t), h->stream));
@@ -674,6 +679,7 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->inst_step.free();
   h->inst_flags.free();
   h->inst_target.free();
+  h->inst_frozen.free();
   h->inst_slot_base.free();
   h->zero_off.free();
   h->events.free();
@@ -1428,17 +1434,33 @@ BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc* d, const
                                   h->cfg.pair_mode == BD_PAIR_CHANNELS);
   if (P.status == BD_ERR_NEGATIVE_RATE || P.status == BD_ERR_ZERO_DIFFUSION || P.status == BD_ERR_ILLEGAL_UNBIND)
     return P.status;
-  std::vector<float4> recs(n);
-  for (size_t i = 0; i < n; i++) {
-    const int s = species[i];
-    const float x = xyz4[4 * i], y = xyz4[4 * i + 1], z = xyz4[4 * i + 2];
-    if (s < 0 || s >= h->S || !(x >= dd.box_lo[0] && x <= dd.box_hi[0] && y >= dd.box_lo[1] && y <= dd.box_hi[1] &&
-                                z >= dd.box_lo[2] && z <= dd.box_hi[2]))
-      return BD_ERR_INVALID_ARGUMENT;
-    uint32_t w = ((uint32_t)k << 16) | (uint32_t)s;
-    float wf;
-    memcpy(&wf, &w, 4);
-    recs[i] = make_float4(x, y, z, wf);
+  // the request's particles: copied whole, checked on the device before
+  // the handle changes, packed into the state after its current records
+  Scratch scratch;
+  UploadArgs up{};
+  if (n) {
+    const uint64_t start[2] = {0, (uint64_t)n};
+    const float box[6] = {dd.box_lo[0], dd.box_lo[1], dd.box_lo[2], dd.box_hi[0], dd.box_hi[1], dd.box_hi[2]};
+    BD_CUDA(scratch.alloc(scratch_bytes({n * sizeof(float4), n * sizeof(int), sizeof(start), sizeof(box),
+                                         sizeof(uint32_t)}),
+                          h->stream));
+    float4* d_xyz4 = scratch.take<float4>(n);
+    int* d_species = scratch.take<int>(n);
+    uint64_t* d_start = scratch.take<uint64_t>(2);
+    float* d_box = scratch.take<float>(6);
+    uint32_t* d_bad = scratch.take<uint32_t>(1);
+    BD_CUDA(cudaMemcpyAsync(d_xyz4, xyz4, n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemcpyAsync(d_species, species, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemcpyAsync(d_start, start, sizeof(start), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemcpyAsync(d_box, box, sizeof(box), cudaMemcpyHostToDevice, h->stream));
+    BD_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(uint32_t), h->stream));
+    up = UploadArgs{d_xyz4, d_species, d_start, d_box, (uint64_t)n, 1, h->S, d_bad, (uint32_t)k};
+    enqueue_upload_check(up, h->stream);
+    BD_CUDA(cudaGetLastError());
+    uint32_t bad = 0;
+    BD_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    BD_CUDA(cudaStreamSynchronize(h->stream));
+    if (bad) return BD_ERR_INVALID_ARGUMENT;
   }
   h->idesc[k] = dd;
   h->derived[k] = P;
@@ -1455,7 +1477,8 @@ BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc* d, const
     if ((st = grow_pairs(h, pc))) return st;
     std::vector<uint32_t> zeros(I, 0);
     if ((st = upload(h->inst_step, zeros, h->stream)) || (st = upload(h->inst_slot_base, zeros, h->stream)) ||
-        (st = upload(h->inst_flags, h->h_flags, h->stream)) || (st = upload(h->inst_target, h->h_target, h->stream)))
+        (st = upload(h->inst_flags, h->h_flags, h->stream)) || (st = upload(h->inst_target, h->h_target, h->stream)) ||
+        (st = upload(h->inst_frozen, zeros, h->stream)))
       return st;
     BD_CUDA(h->zero_off.alloc((size_t)I * h->Z + 1));
     BD_CUDA(cudaMemsetAsync(h->zero_off.p, 0, ((size_t)I * h->Z + 1) * sizeof(uint32_t), h->stream));
@@ -1472,7 +1495,10 @@ BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc* d, const
     if ((st = push_ctrl(h))) return st;
   }
   float4* cur = h->hctrl->cur ? h->state1.p : h->state0.p;
-  if (n) BD_CUDA(cudaMemcpyAsync(cur + n_slots, recs.data(), n * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  if (n) {
+    enqueue_upload_pack(up, cur + n_slots, h->stream);
+    BD_CUDA(cudaGetLastError());
+  }
   BD_CUDA(cudaMemsetAsync(h->events.p + (size_t)k * std::max(h->R, 1), 0,
                           std::max(h->R, 1) * sizeof(unsigned long long), h->stream));
   h->h_flags[k] = kInstActive;
@@ -1531,21 +1557,57 @@ BD_API bd_status bd_instance_harvest(bd_handle h, int k, float* xyz4, int* speci
   if (st && st != BD_ERR_EMPTY) return st;
   const int I = h->n_inst();
   std::vector<uint32_t> base(I), f(I);
+  uint32_t frozen_at = 0;
   BD_CUDA(cudaMemcpy(base.data(), h->inst_slot_base.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
   BD_CUDA(cudaMemcpy(f.data(), h->inst_flags.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(&frozen_at, h->inst_frozen.p + k, sizeof(uint32_t), cudaMemcpyDeviceToHost));
   if (!(f[k] & kInstFrozen)) return BD_ERR_INVALID_ARGUMENT;
   // the instance's records are contiguous: up to the next instance's first slot
   uint64_t end = h->hctrl->n_slots;
   for (int j = 0; j < I; j++)
     if (j != k && h->slot_used[j] && base[j] > base[k] && base[j] < end) end = base[j];
   const uint64_t len = end > base[k] ? end - base[k] : 0;
-  std::vector<float4> r(len);
   const float4* cur = h->hctrl->cur ? h->state1.p : h->state0.p;
-  if (len) BD_CUDA(cudaMemcpy(r.data(), cur + base[k], len * sizeof(float4), cudaMemcpyDeviceToHost));
   // The step's last phase puts reaction products in their reactants' slots,
   // so the state is in canonical order only up to those slots; the next
-  // sort (a frozen step) restores it.  Harvest in canonical order, so the
-  // result does not depend on how many frozen steps ran before it.
+  // sort restores it (a frozen instance neither moves nor reacts).  Harvest
+  // in canonical order, so the result does not depend on how many frozen
+  // steps ran before it: after a frozen step the records are exported as
+  // they lie, on the device; right after the freeze they are sorted here.
+  const bool sorted = (uint32_t)((uint32_t)h->hctrl->step - frozen_at) >= 2u;
+  if (sorted) {
+    const uint32_t tiles = export_tiles(len);
+    Scratch scratch;
+    BD_CUDA(scratch.alloc(scratch_bytes({len * sizeof(float4), len * sizeof(int), tiles * sizeof(uint32_t),
+                                         sizeof(uint32_t)}),
+                          h->stream));
+    ExportArgs a{};
+    a.state = cur + base[k];
+    a.n_slots = len;
+    a.inst = k;
+    a.n_tiles = tiles;
+    a.xyz4 = scratch.take<float4>(len);
+    a.species = scratch.take<int>(len);
+    a.tile_offset = scratch.take<uint32_t>(tiles);
+    a.count = scratch.take<uint32_t>(1);
+    enqueue_export(a, h->stream);
+    BD_CUDA(cudaGetLastError());
+    uint32_t total = 0;
+    BD_CUDA(cudaMemcpyAsync(&total, a.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    BD_CUDA(cudaStreamSynchronize(h->stream));
+    const size_t m = std::min<size_t>(total, cap);
+    if (m && xyz4) BD_CUDA(cudaMemcpyAsync(xyz4, a.xyz4, m * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
+    if (m && species)
+      BD_CUDA(cudaMemcpyAsync(species, a.species, m * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    BD_CUDA(cudaStreamSynchronize(h->stream));
+    *n = total;
+    h->h_flags[k] = f[k] | kInstRemoved;
+    if ((st = put1(h->inst_flags, k, h->h_flags[k], h->stream))) return st;
+    h->slot_free_after[k] = h->hctrl->step;
+    return BD_OK;
+  }
+  std::vector<float4> r(len);
+  if (len) BD_CUDA(cudaMemcpy(r.data(), cur + base[k], len * sizeof(float4), cudaMemcpyDeviceToHost));
   canonical_sort(h->hinst[k], &r);
   size_t m = 0;
   for (const float4& q : r) {

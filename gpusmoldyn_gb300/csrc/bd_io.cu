@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_upload_pack(UploadArgs a, float4* __res
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
     const float4 r = a.xyz4[i];
-    const uint32_t w = ((uint32_t)instance_of(a.start, a.n_inst, i) << 16) | (uint32_t)a.species[i];
+    const uint32_t w = ((a.inst_offset + (uint32_t)instance_of(a.start, a.n_inst, i)) << 16) | (uint32_t)a.species[i];
     out[i] = make_float4(r.x, r.y, r.z, __uint_as_float(w));
   }
 }

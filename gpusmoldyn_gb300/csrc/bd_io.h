@@ -17,6 +17,7 @@ struct UploadArgs {
   uint64_t n;
   int n_inst, n_species;
   uint32_t* bad;  // set to 1 when a particle has a bad species or lies outside its box
+  uint32_t inst_offset;  // instance index of start[0]'s instance in the records' w
 };
 
 // Checks (sets *bad) and packs the staged particles into records

@@ -92,14 +92,19 @@ __device__ __forceinline__ bool advancing(uint32_t flags) {
   return (flags & kInstActive) && !(flags & (kInstFrozen | kInstRemoved));
 }
 
-// Commit one step of an instance; it freezes when it reaches its target, so
-// a request never runs past the step count it asked for.
-__device__ __forceinline__ void advance_instance_step(const KParams& p, uint32_t inst) {
+// Commit one step (global index `step`) of an instance; it freezes when it
+// reaches its target, so a request never runs past the step count it asked
+// for, and the step it froze at is kept (inst_frozen: the state is in
+// canonical order again after one more step).
+__device__ __forceinline__ void advance_instance_step(const KParams& p, uint32_t inst, uint32_t step) {
   const uint32_t f = p.inst_flags[inst];
   if (!advancing(f)) return;
   const uint32_t s = p.inst_step[inst] + 1;
   p.inst_step[inst] = s;
-  if (s >= p.inst_target[inst]) p.inst_flags[inst] = f | kInstFrozen;
+  if (s >= p.inst_target[inst]) {
+    p.inst_flags[inst] = f | kInstFrozen;
+    p.inst_frozen[inst] = step;
+  }
 }
 
 struct Out2 {
@@ -1235,6 +1240,8 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
   __shared__ uint32_t s_more, s_deaths;
   DevCtrl* c = p.ctrl;
   if (ld_u32(&c->status)) return;
+  // read before the barriers below; thread 0 advances it at the end
+  const uint32_t step_now = (uint32_t)*(volatile uint64_t*)&c->step;
   const uint32_t K = ld_u32(&c->n_pairs);
   if (K > p.pair_cap) {
     if (threadIdx.x == 0) atomicOr(&c->status, kStatPairs);
@@ -1343,7 +1350,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
   commit_events(p);
   for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) {
     const DevInstance& I = p.inst[inst];
-    advance_instance_step(p, inst);
+    advance_instance_step(p, inst, step_now);
     p.inst_slot_base[inst] = p.cell_start[I.cell_base];
   }
   if (threadIdx.x == 0) {
@@ -1392,8 +1399,10 @@ __global__ void __launch_bounds__(256) k_append(KParams p) {
 __global__ void k_finalize_inplace(KParams p) {
   DevCtrl* c = p.ctrl;
   if (ld_u32(&c->status)) return;
+  const uint32_t step_now = (uint32_t)*(volatile uint64_t*)&c->step;
   commit_events(p);
-  for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) advance_instance_step(p, inst);
+  for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) advance_instance_step(p, inst, step_now);
+  __syncthreads();  // every thread has read the step before thread 0 advances it
   if (threadIdx.x == 0) {
     c->n_slots += c->n_virtual;
     c->n_virtual = 0;

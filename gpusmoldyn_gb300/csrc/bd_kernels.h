@@ -25,6 +25,7 @@ struct KParams {
   uint32_t* inst_step;        // [I] steps taken by each instance
   uint32_t* inst_flags;       // [I] InstanceFlags (frozen on device at the target)
   const uint32_t* inst_target;// [I] step count at which an instance freezes
+  uint32_t* inst_frozen;      // [I] global step (low 32 bits) at which an instance froze
   uint32_t* inst_slot_base;   // [I] first slot of each instance in the current state
   uint32_t* zero_off;         // [I*Z + 1] prefix of zeroth-order births
   uint32_t* cell_count;       // [n_cells] particles per cell (returns to 0 each step)

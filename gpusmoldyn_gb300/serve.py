@@ -6,7 +6,9 @@ slot and the HBM budget allow, advances every admitted simulation together
 by a chunk of steps (one pipeline over all of them, one graph launch per
 step), then harvests the simulations that reached their step count.  A
 simulation freezes on the device at exactly its step count, so chunking
-never overshoots, and it evolves bit for bit as it would alone.
+never overshoots, and it evolves bit for bit as it would alone.  It is
+harvested one chunk after it freezes: by then a step has put its records
+back in canonical order on the device, and the harvest is a device export.
 """
 from __future__ import annotations
 
@@ -59,7 +61,9 @@ class Server:
         active = {}  # slot -> (job, bytes)
         used = 0.0
         done = []
+        seen = set()  # slots reported finished by the previous poll
         psteps = 0.0
+        spent = collections.defaultdict(float)  # host seconds per activity
         t0 = time.perf_counter()
         while pending or waiting or active:
             now = time.perf_counter() - t0
@@ -71,8 +75,12 @@ class Server:
                 if used + need > self.budget and active:
                     break
                 waiting.popleft()
-                desc, pos, sp, steps = make_request(job)
+                ta = time.perf_counter()
+                desc, pos, sp, steps = job["payload"] if "payload" in job else make_request(job)
+                tb = time.perf_counter()
                 slot = s.admit(desc, pos, sp, steps)
+                spent["make_request"] += tb - ta
+                spent["admit"] += time.perf_counter() - tb
                 job["admitted"] = time.perf_counter() - t0
                 active[slot] = (job, need)
                 used += need
@@ -81,12 +89,21 @@ class Server:
                     time.sleep(max(0.0, pending[0]["arrival"] * time_scale - (time.perf_counter() - t0)))
                 continue
             live = sum(j["n"] for j, _ in active.values())
+            ta = time.perf_counter()
             s.step(self.chunk)
             s.synchronize()
+            tb = time.perf_counter()
+            spent["steps"] += tb - ta
             psteps += live * self.chunk
-            for slot in s.poll():
+            finished = s.poll()
+            spent["poll"] += time.perf_counter() - tb
+            ready = [slot for slot in finished if slot in seen]
+            seen = set(finished) - set(ready)
+            for slot in ready:
                 job, need = active.pop(slot)
+                tc = time.perf_counter()
                 pos, sp = s.harvest(slot)
+                spent["harvest"] += time.perf_counter() - tc
                 job["finished"] = time.perf_counter() - t0
                 job["latency"] = job["finished"] - job["arrival"] * time_scale
                 job["n_final"] = int(len(sp))
@@ -99,7 +116,8 @@ class Server:
         work = float(sum(j["n"] * j["steps"] for j in done))
         return dict(jobs=len(done), wall_s=wall, p50_s=float(np.percentile(lat, 50)),
                     p99_s=float(np.percentile(lat, 99)), mean_s=float(lat.mean()),
-                    particle_steps_per_s=work / wall, approx_device_particle_steps=psteps, done=done)
+                    particle_steps_per_s=work / wall, approx_device_particle_steps=psteps, done=done,
+                    host_seconds=dict(spent))
 
     def close(self):
         self.s.close()

@@ -363,19 +363,14 @@ class System:
         return [int(v) for v in buf[:m.value]]
 
     def harvest(self, slot):
-        cap = 1 << 16
-        while True:
-            pos = np.zeros((cap, 4), np.float32)
-            sp = np.zeros(cap, np.int32)
-            n = C.c_size_t()
-            # harvest copies and frees in one call, so size the buffer first
-            steps, flags = self.instance_state(slot)
-            cnt = int(self.instance_counts()[slot])
-            if cnt > cap:
-                cap = cnt
-                continue
-            L.check(self.lib.bd_instance_harvest(self.h, slot, _ptr(pos), _ptr(sp), cap, C.byref(n)), "harvest")
-            return pos[:n.value, :3].copy(), sp[:n.value].copy()
+        # harvest copies and frees in one call, so size the buffer first
+        cap = max(int(self.instance_counts()[slot]), 1)
+        pos = np.empty((cap, 4), np.float32)
+        sp = np.empty(cap, np.int32)
+        n = C.c_size_t()
+        L.check(self.lib.bd_instance_harvest(self.h, slot, _ptr(pos), _ptr(sp), cap, C.byref(n)), "harvest")
+        m = min(n.value, cap)
+        return np.ascontiguousarray(pos[:m, :3]), sp[:m]
 
     def instance_state(self, slot):
         s, f = C.c_uint32(), C.c_uint32()

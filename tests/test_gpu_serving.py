@@ -96,3 +96,29 @@ def test_server_slots_are_reused():
         s.step(1)  # drops the harvested records, frees the slots
         s.synchronize()
     s.close()
+
+
+def test_harvest_after_frozen_steps_equals_harvest_at_the_freeze():
+    """Right after the freeze the harvest sorts on the host (products still
+    sit in their reactants' slots); after a frozen step the records are in
+    canonical order on the device and the harvest exports them as they lie.
+    Both give the same particles, in the same order."""
+    results = []
+    for extra in (0, 1, 5):
+        s = System(dt=1e-3, instances=2)
+        network(s)
+        desc, pos, sp, steps = job(1)
+        slot = s.admit(desc, pos, sp, steps)
+        other = s.admit(*job(0))  # a neighbour that keeps running
+        s.step(steps)
+        s.synchronize()
+        assert slot in s.poll()
+        s.step(extra)
+        s.synchronize()
+        results.append(s.harvest(slot))
+        s.close()
+        del other
+    for pos, sp in results[1:]:
+        np.testing.assert_array_equal(pos, results[0][0])
+        np.testing.assert_array_equal(sp, results[0][1])
+    assert len(results[0][1]) > 1000
