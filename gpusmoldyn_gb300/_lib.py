@@ -155,6 +155,8 @@ _SIGS = {
     "bd_cell_sort_static": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.POINTER(C.c_uint32), P, P, P]),
     "bd_get_config": (C.c_int, [H, C.POINTER(bd_config)]),
+    "bd_save_checkpoint": (C.c_int, [H, C.c_char_p]),
+    "bd_load_checkpoint": (C.c_int, [H, C.c_char_p]),
     "bd_add_surface": (C.c_int, [H, C.POINTER(C.c_int)]),
     "bd_set_surface_action": (C.c_int, [H, C.c_int, C.c_int, C.c_int, C.c_int]),
     "bd_get_surface_action": (C.c_int, [H, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),

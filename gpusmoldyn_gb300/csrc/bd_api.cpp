@@ -9,6 +9,7 @@
 // (a step that overflows writes only into buffers that the next attempt
 // overwrites, so replay is exact).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -41,6 +42,15 @@ bool cuda_ok(cudaError_t e, const char* what) {
   g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
   return false;
 }
+
+// NVTX range over one C-ABI call (host timeline of nsys / ncu; a no-op
+// without a tool attached).  The step graphs' kernels carry their own names.
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
 
 #define BD_CUDA(call)                                   \
   do {                                                  \
@@ -535,6 +545,7 @@ size_t scratch_bytes(std::initializer_list<size_t> sizes) {
 // range, inside the instance's box) before anything of the handle changes,
 // and packed into records by a kernel.
 bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, const uint64_t* counts) {
+  const Range range("bd_set_particles");
   if (!h->finalized) return BD_ERR_NOT_FINALIZED;
   const int I = h->n_inst();
   uint64_t n = 0;
@@ -927,6 +938,7 @@ BD_API bd_status bd_set_reaction_probability(bd_handle h, int rxn, float prob) {
 }
 
 BD_API bd_status bd_finalize(bd_handle h) {
+  const Range range("bd_finalize");
   if (!h) return BD_ERR_INVALID_ARGUMENT;
   if (h->finalized) return BD_ERR_ALREADY_FINALIZED;
   if (h->D.empty()) return BD_ERR_INVALID_ARGUMENT;
@@ -1118,6 +1130,7 @@ BD_API bd_status bd_set_ensemble_particles(bd_handle h, const float* xyz4, const
 }
 
 BD_API bd_status bd_step(bd_handle h, int nsteps) {
+  const Range range("bd_step");
   if (!h || nsteps < 0) return BD_ERR_INVALID_ARGUMENT;
   if (!h->finalized) return BD_ERR_NOT_FINALIZED;
   if (h->host_only) return BD_ERR_NO_DEVICE;
@@ -1138,6 +1151,7 @@ BD_API bd_status bd_step(bd_handle h, int nsteps) {
 }
 
 BD_API bd_status bd_step_async(bd_handle h, int nsteps, void* stream) {
+  const Range range("bd_step_async");
   if (!h || nsteps < 0) return BD_ERR_INVALID_ARGUMENT;
   if (h->host_only) return BD_ERR_NO_DEVICE;
   BD_CUDA(cudaSetDevice(h->device));
@@ -1162,6 +1176,7 @@ BD_API bd_status bd_step_async(bd_handle h, int nsteps, void* stream) {
 }
 
 BD_API bd_status bd_synchronize(bd_handle h) {
+  const Range range("bd_synchronize");
   if (!h) return BD_ERR_INVALID_ARGUMENT;
   if (!h->have_particles) return BD_OK;
   BD_CUDA(cudaSetDevice(h->device));
@@ -1267,6 +1282,7 @@ BD_API bd_status bd_get_particles(bd_handle h, float* xyz4, int* species, size_t
 
 BD_API bd_status bd_get_instance_particles(bd_handle h, int inst, float* xyz4, int* species, size_t cap,
                                            size_t* n) {
+  const Range range("bd_get_particles");
   if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
   if (inst >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
   *n = 0;
@@ -1404,6 +1420,7 @@ bd_status put1(DevBuf<T>& buf, int k, T v, cudaStream_t s) {
 
 BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc* d, const float* xyz4, const int* species,
                                    size_t n, uint32_t steps, int* slot_out) {
+  const Range range("bd_instance_admit");
   if (!h || !h->server || !d || !slot_out || steps == 0 || (n > 0 && (!xyz4 || !species)))
     return BD_ERR_INVALID_ARGUMENT;
   if (!h->finalized) return BD_ERR_NOT_FINALIZED;
@@ -1550,6 +1567,7 @@ BD_API bd_status bd_instance_poll(bd_handle h, int* slots, int cap, int* n_finis
 }
 
 BD_API bd_status bd_instance_harvest(bd_handle h, int k, float* xyz4, int* species, size_t cap, size_t* n) {
+  const Range range("bd_instance_harvest");
   if (!h || !h->server || !n || k < 0 || k >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
   *n = 0;
   if (!h->slot_used[k] || h->slot_free_after[k] != UINT64_MAX) return BD_ERR_INVALID_ARGUMENT;
@@ -1908,6 +1926,165 @@ bd_status find_name(const std::vector<std::string>& names, const char* name, int
   return BD_ERR_INVALID_ARGUMENT;
 }
 }  // namespace
+
+// ------------------------------------------------------------ checkpoints
+namespace {
+
+constexpr char kCkptMagic[8] = {'B', 'D', 'C', 'K', 'P', 'T', '0', '1'};
+
+// What a handle must match to load a checkpoint: the network's shape and
+// time step, the normal and pair modes, each instance's box, seed and scales.
+std::vector<uint8_t> fingerprint(const bd_system* h) {
+  std::vector<uint8_t> f;
+  auto put = [&f](const void* p, size_t n) {
+    const uint8_t* b = (const uint8_t*)p;
+    f.insert(f.end(), b, b + n);
+  };
+  const int32_t shape[6] = {h->S, h->R, h->n_inst(), h->cfg.normal_mode, (int32_t)h->cfg.pair_mode,
+                            (int32_t)h->panels.size()};
+  put(shape, sizeof(shape));
+  put(&h->cfg.dt, sizeof(float));
+  put(h->D.data(), h->D.size() * sizeof(float));
+  for (const ReactionDef& r : h->rx) {
+    const int32_t v[5] = {r.order, r.reactants[0], r.reactants[1], r.products[0], r.products[1]};
+    put(v, sizeof(v));
+    put(&r.rate, sizeof(r.rate));
+  }
+  for (const bd_instance_desc& d : h->idesc) {
+    put(d.box_lo, sizeof(d.box_lo));
+    put(d.box_hi, sizeof(d.box_hi));
+    put(&d.seed, sizeof(d.seed));
+    put(&d.d_scale, sizeof(float));
+    put(&d.k2_scale, sizeof(float));
+    put(&d.cell_size, sizeof(float));
+  }
+  return f;
+}
+
+struct File {
+  FILE* f = nullptr;
+  ~File() {
+    if (f) fclose(f);
+  }
+};
+
+}  // namespace
+
+BD_API bd_status bd_save_checkpoint(bd_handle h, const char* path) {
+  const Range range("bd_save_checkpoint");
+  if (!h || !path || h->server) return BD_ERR_INVALID_ARGUMENT;
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  if (!h->have_particles) return BD_ERR_NOT_FINALIZED;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  const int I = h->n_inst();
+  const DevCtrl c = *h->hctrl;
+  std::vector<float4> slots(c.n_slots);
+  std::vector<uint32_t> step(I), flags(I), target(I), base(I);
+  std::vector<unsigned long long> events((size_t)I * std::max(h->R, 1));
+  const float4* cur = c.cur ? h->state1.p : h->state0.p;
+  if (c.n_slots) BD_CUDA(cudaMemcpy(slots.data(), cur, slots.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(step.data(), h->inst_step.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(flags.data(), h->inst_flags.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(target.data(), h->inst_target.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(base.data(), h->inst_slot_base.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  BD_CUDA(cudaMemcpy(events.data(), h->events.p, events.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  const std::vector<uint8_t> fp = fingerprint(h);
+  File out;
+  out.f = fopen(path, "wb");
+  if (!out.f) return BD_ERR_INVALID_ARGUMENT;
+  const uint64_t head[5] = {(uint64_t)fp.size(), c.step, c.n_slots, c.deaths_last, (uint64_t)I};
+  bool ok = fwrite(kCkptMagic, 8, 1, out.f) == 1 && fwrite(head, sizeof(head), 1, out.f) == 1 &&
+            (fp.empty() || fwrite(fp.data(), fp.size(), 1, out.f) == 1);
+  for (int k = 0; k < I && ok; k++) {
+    const uint64_t planned = k < (int)h->plan_n.size() ? h->plan_n[k] : 0;
+    const uint32_t v[4] = {step[k], flags[k], target[k], base[k]};
+    ok = fwrite(&planned, sizeof(planned), 1, out.f) == 1 && fwrite(v, sizeof(v), 1, out.f) == 1;
+  }
+  ok = ok && fwrite(events.data(), sizeof(unsigned long long), events.size(), out.f) == events.size();
+  ok = ok && (slots.empty() || fwrite(slots.data(), sizeof(float4), slots.size(), out.f) == slots.size());
+  ok = (fclose(out.f) == 0) && ok;
+  out.f = nullptr;
+  return ok ? BD_OK : BD_ERR_INVALID_ARGUMENT;
+}
+
+BD_API bd_status bd_load_checkpoint(bd_handle h, const char* path) {
+  const Range range("bd_load_checkpoint");
+  if (!h || !path || h->server) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  File in;
+  in.f = fopen(path, "rb");
+  if (!in.f) return BD_ERR_INVALID_ARGUMENT;
+  char magic[8];
+  uint64_t head[5];
+  if (fread(magic, 8, 1, in.f) != 1 || memcmp(magic, kCkptMagic, 8) != 0 || fread(head, sizeof(head), 1, in.f) != 1)
+    return BD_ERR_INVALID_ARGUMENT;
+  const std::vector<uint8_t> fp = fingerprint(h);
+  const int I = h->n_inst();
+  if (head[0] != fp.size() || head[4] != (uint64_t)I || head[2] > 0xFFFFFFF0ull) {
+    g_last_error = "checkpoint of a differently built handle";
+    return BD_ERR_INVALID_ARGUMENT;
+  }
+  std::vector<uint8_t> fp_file(fp.size());
+  if ((!fp.empty() && fread(fp_file.data(), fp.size(), 1, in.f) != 1) || fp_file != fp) {
+    g_last_error = "checkpoint of a differently built handle";
+    return BD_ERR_INVALID_ARGUMENT;
+  }
+  const uint64_t n_slots = head[2];
+  std::vector<uint64_t> planned(I);
+  std::vector<uint32_t> step(I), flags(I), target(I), base(I);
+  for (int k = 0; k < I; k++) {
+    uint32_t v[4];
+    if (fread(&planned[k], sizeof(uint64_t), 1, in.f) != 1 || fread(v, sizeof(v), 1, in.f) != 1)
+      return BD_ERR_INVALID_ARGUMENT;
+    step[k] = v[0], flags[k] = v[1], target[k] = v[2], base[k] = v[3];
+  }
+  std::vector<unsigned long long> events((size_t)I * std::max(h->R, 1));
+  std::vector<float4> slots(n_slots);
+  if (fread(events.data(), sizeof(unsigned long long), events.size(), in.f) != events.size() ||
+      (n_slots && fread(slots.data(), sizeof(float4), n_slots, in.f) != n_slots))
+    return BD_ERR_INVALID_ARGUMENT;
+  BD_CUDA(cudaSetDevice(h->device));
+  if (h->have_particles) {
+    const bd_status st = bd_synchronize(h);
+    if (st && st != BD_ERR_EMPTY) return st;
+  }
+  // the grids the original planned, then the buffers and the state
+  h->hinst.assign(I, DevInstance{});
+  for (int k = 0; k < I; k++) plan_instance(h, k, planned[k]);
+  bd_status st = layout_cells(h);
+  if (st) return st;
+  uint64_t cap = h->cfg.capacity ? h->cfg.capacity : std::max<uint64_t>(2 * n_slots, 4096);
+  cap = std::max<uint64_t>(cap, n_slots);
+  h->have_particles = false;
+  memset(h->hctrl, 0, sizeof(DevCtrl));
+  if ((st = grow_particles(h, cap))) return st;
+  const uint32_t pc = h->cfg.pair_capacity ? h->cfg.pair_capacity : (uint32_t)std::max<uint64_t>(65536, cap / 32);
+  if ((st = grow_pairs(h, pc))) return st;
+  if (n_slots)
+    BD_CUDA(cudaMemcpyAsync(h->state0.p, slots.data(), n_slots * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  h->h_flags = flags;
+  h->h_target = target;
+  std::vector<uint32_t> zeros(I, 0);
+  if ((st = upload(h->inst_step, step, h->stream)) || (st = upload(h->inst_slot_base, base, h->stream)) ||
+      (st = upload(h->inst_flags, flags, h->stream)) || (st = upload(h->inst_target, target, h->stream)) ||
+      (st = upload(h->inst_frozen, zeros, h->stream)) || (st = upload(h->events, events, h->stream)))
+    return st;
+  BD_CUDA(h->zero_off.alloc((size_t)I * h->Z + 1));
+  BD_CUDA(cudaMemsetAsync(h->zero_off.p, 0, ((size_t)I * h->Z + 1) * sizeof(uint32_t), h->stream));
+  BD_CUDA(h->pending.alloc((size_t)I * std::max(h->R, 1)));
+  BD_CUDA(cudaMemsetAsync(h->pending.p, 0, h->pending.n * sizeof(unsigned long long), h->stream));
+  memset(h->hctrl, 0, sizeof(DevCtrl));
+  h->hctrl->n_slots = (uint32_t)n_slots;
+  h->hctrl->step = head[1];
+  h->hctrl->deaths_last = (uint32_t)head[3];
+  if ((st = push_ctrl(h))) return st;
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  h->have_particles = true;
+  h->target_step = head[1];
+  return build_graphs(h);
+}
 
 BD_API bd_status bd_get_config(bd_handle h, bd_config* out) {
   if (!h || !out) return BD_ERR_INVALID_ARGUMENT;

@@ -399,6 +399,14 @@ class System:
         L.check(self.lib.bd_get_kernels_per_step(self.h, C.byref(k)), "kernels_per_step")
         return k.value
 
+    def save_checkpoint(self, path):
+        """The whole dynamic state, to resume bit for bit (bd_save_checkpoint)."""
+        L.check(self.lib.bd_save_checkpoint(self.h, str(path).encode()), "bd_save_checkpoint")
+
+    def load_checkpoint(self, path):
+        """Resume from save_checkpoint's file on a handle built the same way."""
+        L.check(self.lib.bd_load_checkpoint(self.h, str(path).encode()), "bd_load_checkpoint")
+
     def write_snapshot(self, path, binary=False):
         """Write the molecules to `path` (bd_write_snapshot)."""
         L.check(self.lib.bd_write_snapshot(self.h, str(path).encode(), 1 if binary else 0), "write_snapshot")

@@ -436,6 +436,18 @@ BD_API bd_status bd_get_surface_counts(bd_handle h, int *n_surfaces, int *n_pane
 enum { BD_SNAPSHOT_TEXT = 0, BD_SNAPSHOT_BINARY = 1 };
 BD_API bd_status bd_write_snapshot(bd_handle h, const char *path, int format);
 
+/* ---------------------------------------------------------- checkpoints */
+/* The whole dynamic state of a handle, to stop a run and resume it: every
+ * slot in slot order (empty ones too), the step counters of the handle and
+ * of each instance, the event counters, and the particle counts each
+ * instance's grid was planned for.  A handle built the same way (network,
+ * configuration and instances; checked against a fingerprint stored in the
+ * file) and loaded from it continues bit for bit as the original would
+ * have.  The reference has no checkpoint (its debug dumps, particleSystem.
+ * cpp:1003-1030, cannot be read back).  Not for serving handles. */
+BD_API bd_status bd_save_checkpoint(bd_handle h, const char *path);
+BD_API bd_status bd_load_checkpoint(bd_handle h, const char *path);
+
 /* The configuration a handle was created with (box, dt, seed, ...). */
 BD_API bd_status bd_get_config(bd_handle h, bd_config *out);
 
