@@ -690,16 +690,25 @@ struct Seeker {
 // False when the record takes no part in this step's pair search: born in
 // this step, instance not advancing, or a species without second-order
 // reactions.
+// s_maxr (one-instance kernels): the species' largest radii in shared
+// memory, with adv0 the instance's advancing state, read once per kernel.
 template <bool kSingle>
-__device__ __forceinline__ bool seeker_init(const KParams& p, const float4& r, Seeker& k) {
+__device__ __forceinline__ bool seeker_init(const KParams& p, const float4& r, Seeker& k,
+                                            const float* s_maxr = nullptr, bool adv0 = true) {
   const uint32_t w = rec_w(r);
   if (w & kNewborn) return false;
   k.r = r;
   k.inst = w >> 16;
-  if (!advancing(__ldg(&p.inst_flags[k.inst]))) return false;
-  k.block = inst_of<kSingle>(p, k.inst).block;
   const uint32_t sa = w & kSpeciesMask;
-  k.max_r = __ldg(&p.species[k.block * p.S + sa].max_r);
+  if (kSingle && s_maxr) {
+    if (!adv0) return false;
+    k.block = p.inst0.block;
+    k.max_r = s_maxr[sa];
+  } else {
+    if (!advancing(__ldg(&p.inst_flags[k.inst]))) return false;
+    k.block = inst_of<kSingle>(p, k.inst).block;
+    k.max_r = __ldg(&p.species[k.block * p.S + sa].max_r);
+  }
   // a bound on every squared radius of the species (float rounding of max_r^2)
   k.r2max = k.max_r * k.max_r * 1.0001f;
   // fl(dx^2) <= d2 <= r2max, so |dx| <= max_r * 1.00005
@@ -858,6 +867,12 @@ template <bool kHasBim, bool kBinned, bool kSingle>
 __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   __shared__ uint32_t s_cell[8][32], s_cs[8][32], s_n[8][32], s_off[8][32];
   __shared__ VisitQueue s_visit[kHasBim ? 8 : 1];
+  __shared__ float s_maxr[kSingle ? kCtxSpecies : 1];
+  if (kSingle) {  // before any warp may leave: one barrier for the whole CTA
+    for (uint32_t t = threadIdx.x; t < p.S; t += blockDim.x) s_maxr[t] = p.species[p.inst0.block * p.S + t].max_r;
+    __syncthreads();
+  }
+  const bool adv0 = kSingle ? advancing(ld_u32(&p.inst_flags[0])) : true;
   DevCtrl* c = p.ctrl;
   if (ctrl_status_warp(c)) return;
   const uint32_t cur = ld_u32(&c->cur);
@@ -915,20 +930,23 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
         const float4* __restrict__ cb = cell_records<kBinned>(p, ocell, ocs);
         ra = __ldg(&cb[j]);
         Seeker k;
-        const bool search = kHasBim && seeker_init<kSingle>(p, ra, k);
+        const bool search = kHasBim && seeker_init<kSingle>(p, ra, k, kSingle ? s_maxr : nullptr, adv0);
         const float xlim = search ? k.xlim : -1.0f;
         const uint32_t rx = __float_as_uint(ra.x);
         const float* __restrict__ cbx = reinterpret_cast<const float*>(cb);
-        uint32_t rank = 0, cand = 0;  // cand: bit m = later member m < 32 with |dx| within range
-        bool tie = false;
+        // rank: members with smaller x bits; le also counts equal ones (the
+        // record itself among them), so le - rank > 1 means a tie to break
+        // on all four words.  cand: bit m = member m < 32 with |dx| in range
+        uint32_t rank = 0, le = 0, cand = 0;
         for (uint32_t m = 0; m < on; ++m) {
           const float qx = __ldg(&cbx[4 * m]);
           const uint32_t qb = __float_as_uint(qx);
           rank += qb < rx ? 1u : 0u;
-          tie |= qb == rx && m != j;
-          if (m > j && m < 32u && fabsf(__fsub_rn(qx, ra.x)) <= xlim) cand |= 1u << m;
+          le += qb <= rx ? 1u : 0u;
+          if (m < 32u && fabsf(__fsub_rn(qx, ra.x)) <= xlim) cand |= 1u << m;
         }
-        if (tie) rank = canonical_rank(cb, 0, on, j, ra);
+        cand &= j >= 31u ? 0u : ~((2u << j) - 1u);  // later members only
+        if (le - rank > 1u) rank = canonical_rank(cb, 0, on, j, ra);
         ca = ocs + rank;
         if (ca < p.capacity) nx[ca] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
         else atomicOr(&c->status, kStatBounds);
