@@ -804,9 +804,9 @@ __device__ __forceinline__ uint32_t forward_key(uint32_t key0, uint32_t b, uint3
 // nkey, found from r's side.
 template <bool kBinned, bool kSingle>
 __device__ __forceinline__ void visit_neighbour(const KParams& p, DevCtrl* c, const float4& r, uint32_t ca,
-                                                uint32_t nkey) {
+                                                uint32_t nkey, const float* s_maxr = nullptr, bool adv0 = true) {
   Seeker k;
-  if (!seeker_init<kSingle>(p, r, k)) return;
+  if (!seeker_init<kSingle>(p, r, k, s_maxr, adv0)) return;
   const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
   if (nn > kBigCell) return;  // pairs with large cells are found by k_pairs_big_pairs
   const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
@@ -848,7 +848,8 @@ struct VisitQueue {
 // Visit the first 32 queued entries, one per lane, and move the rest
 // (vq - 32 < 32 entries) to the front.  Warp-uniform call.
 template <bool kBinned, bool kSingle>
-__device__ __forceinline__ void drain_visits(const KParams& p, DevCtrl* c, VisitQueue& q, uint32_t vq) {
+__device__ __forceinline__ void drain_visits(const KParams& p, DevCtrl* c, VisitQueue& q, uint32_t vq,
+                                             const float* s_maxr, bool adv0) {
   const uint32_t lane = lane_id();
   __syncwarp();
   const float4 r = q.rec[lane];
@@ -860,12 +861,12 @@ __device__ __forceinline__ void drain_visits(const KParams& p, DevCtrl* c, Visit
     q.key[lane] = q.key[lane + 32u];
   }
   __syncwarp();
-  visit_neighbour<kBinned, kSingle>(p, c, r, ca, key);
+  visit_neighbour<kBinned, kSingle>(p, c, r, ca, key, s_maxr, adv0);
 }
 
 template <bool kHasBim, bool kBinned, bool kSingle>
 __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
-  __shared__ uint32_t s_cell[8][32], s_cs[8][32], s_n[8][32], s_off[8][32];
+  __shared__ uint4 s_cells[8][32];  // per non-empty cell of the task: key, first slot, records, offset
   __shared__ VisitQueue s_visit[kHasBim ? 8 : 1];
   __shared__ float s_maxr[kSingle ? kCtxSpecies : 1];
   if (kSingle) {  // before any warp may leave: one barrier for the whole CTA
@@ -910,12 +911,7 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
       if (lane >= (uint32_t)d) incl += t;
     }
     const uint32_t off = incl - n, total = __shfl_sync(kFull, incl, 31);
-    if (n > 0) {
-      s_cell[warp][q] = cell;
-      s_cs[warp][q] = cs;
-      s_n[warp][q] = n;
-      s_off[warp][q] = off;
-    }
+    if (n > 0) s_cells[warp][q] = make_uint4(cell, cs, n, off);
     __syncwarp();
     uint32_t before = 0;  // non-empty cells that start before this round
     for (uint32_t rb = 0; rb < total; rb += 32u) {
@@ -925,8 +921,9 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
       float4 ra = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (t < total) {
         const uint32_t oq = before + __popc(M & le_mask) - 1u;
-        const uint32_t ocell = s_cell[warp][oq], ocs = s_cs[warp][oq], on = s_n[warp][oq];
-        const uint32_t j = t - s_off[warp][oq];
+        const uint4 cc = s_cells[warp][oq];
+        const uint32_t ocell = cc.x, ocs = cc.y, on = cc.z;
+        const uint32_t j = t - cc.w;
         const float4* __restrict__ cb = cell_records<kBinned>(p, ocell, ocs);
         ra = __ldg(&cb[j]);
         Seeker k;
@@ -985,7 +982,7 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
           }
           vq += __popc(ball);
           if (vq >= 32u) {
-            drain_visits<kBinned, kSingle>(p, c, vqueue, vq);
+            drain_visits<kBinned, kSingle>(p, c, vqueue, vq, kSingle ? s_maxr : nullptr, adv0);
             vq -= 32u;
           }
         }
@@ -996,7 +993,9 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   }
   if (kHasBim) {
     __syncwarp();
-    if (lane < vq) visit_neighbour<kBinned, kSingle>(p, c, vqueue.rec[lane], vqueue.ca[lane], vqueue.key[lane]);
+    if (lane < vq)
+      visit_neighbour<kBinned, kSingle>(p, c, vqueue.rec[lane], vqueue.ca[lane], vqueue.key[lane],
+                                        kSingle ? s_maxr : nullptr, adv0);
   }
 }
 
