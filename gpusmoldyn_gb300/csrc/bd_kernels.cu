@@ -497,6 +497,18 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
   });
 }
 
+// Bin layout.  Record-major: place `off` of every cell is one contiguous
+// array, bins[off * n_cells + cell].  The records a warp bins belong to a
+// few consecutive cells (the state is in cell order), so their stores, and
+// the pair kernel's loads of the same place across 32 consecutive cells,
+// fall on a few contiguous lines; cell-major bins (bins[cell * bin_cap +
+// off]) put each cell on its own line.
+constexpr bool kBinRecordMajor = true;
+
+__device__ __forceinline__ size_t bin_index(const KParams& p, uint32_t cell, uint32_t off) {
+  return kBinRecordMajor ? (size_t)off * p.n_cells + cell : (size_t)cell * p.bin_cap + off;
+}
+
 // A record waiting for its place in a bin: the warp's claim (atomicAdd on
 // the cell count by the lane that leads the cell's peers) is issued when
 // the record is made and consumed one record later, so the atomic's round
@@ -525,7 +537,7 @@ __device__ __forceinline__ void claim_retire(const KParams& p, DevCtrl* c, const
   const uint32_t off = __shfl_sync(kFull, pc.old, pc.leader) + pc.rank;
   if (pc.key == kNoKey) return;
   if (off < p.bin_cap) {
-    p.bins[(size_t)pc.key * p.bin_cap + off] = pc.r;
+    p.bins[bin_index(p, pc.key, off)] = pc.r;
   } else {
     atomicOr(&c->status, kStatBins);
     atomicMax(&c->bin_need, off + 1u);
@@ -635,10 +647,23 @@ __global__ void __launch_bounds__(256, 2) k_bin_surface(KParams p) {
   }
 }
 
+// The records of one cell, m-th at base[m * stride]: a bin of the binned
+// sort (record-major bins: stride = the number of cells) or a range of the
+// compact scatter buffer (stride 1).
+struct CellView {
+  const float4* base;
+  size_t stride;
+  __device__ __forceinline__ float4 operator[](uint32_t m) const { return base[(size_t)m * stride]; }
+  __device__ __forceinline__ float4 ldg(uint32_t m) const { return __ldg(base + (size_t)m * stride); }
+  __device__ __forceinline__ float ldg_x(uint32_t m) const {
+    return __ldg(reinterpret_cast<const float*>(base + (size_t)m * stride));
+  }
+};
+
 // Position of record r among the records of its cell [s, e) in canonical
 // order; ties between identical records go by slot.
-__device__ __forceinline__ uint32_t canonical_rank(const float4* __restrict__ sc, uint32_t s, uint32_t e,
-                                                   uint32_t slot, const float4& r) {
+__device__ __forceinline__ uint32_t canonical_rank(const CellView sc, uint32_t s, uint32_t e, uint32_t slot,
+                                                   const float4& r) {
   uint32_t rank = 0;
   for (uint32_t m = s; m < e; ++m) {
     const float4 q = sc[m];
@@ -674,8 +699,9 @@ constexpr int kBigGrid = 304;  // CTAs of the large-cell kernels (cells they tak
 
 // First record of a cell: its bin, or its range of the compact scatter buffer.
 template <bool kBinned>
-__device__ __forceinline__ const float4* cell_records(const KParams& p, uint32_t cell, uint32_t cs) {
-  return kBinned ? p.bins + (size_t)cell * p.bin_cap : p.scatter + cs;
+__device__ __forceinline__ CellView cell_records(const KParams& p, uint32_t cell, uint32_t cs) {
+  if (kBinned) return CellView{p.bins + bin_index(p, cell, 0), kBinRecordMajor ? (size_t)p.n_cells : 1u};
+  return CellView{p.scatter + cs, 1u};
 }
 
 // A record looking for partners.
@@ -809,9 +835,9 @@ __device__ __forceinline__ void visit_neighbour(const KParams& p, DevCtrl* c, co
   if (!seeker_init<kSingle>(p, r, k, s_maxr, adv0)) return;
   const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
   if (nn > kBigCell) return;  // pairs with large cells are found by k_pairs_big_pairs
-  const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
+  const CellView nb = cell_records<kBinned>(p, nkey, ns);
   for (uint32_t m = 0; m < nn; ++m) {
-    const float4 q = __ldg(&nb[m]);
+    const float4 q = nb.ldg(m);
     const int32_t b = pair_reaction(p, k, q);
     if (b >= 0) emit<kSingle>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
   }
@@ -924,19 +950,33 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
         const uint4 cc = s_cells[warp][oq];
         const uint32_t ocell = cc.x, ocs = cc.y, on = cc.z;
         const uint32_t j = t - cc.w;
-        const float4* __restrict__ cb = cell_records<kBinned>(p, ocell, ocs);
-        ra = __ldg(&cb[j]);
+        const CellView cb = cell_records<kBinned>(p, ocell, ocs);
+        ra = cb.ldg(j);
         Seeker k;
         const bool search = kHasBim && seeker_init<kSingle>(p, ra, k, kSingle ? s_maxr : nullptr, adv0);
         const float xlim = search ? k.xlim : -1.0f;
         const uint32_t rx = __float_as_uint(ra.x);
-        const float* __restrict__ cbx = reinterpret_cast<const float*>(cb);
         // rank: members with smaller x bits; le also counts equal ones (the
         // record itself among them), so le - rank > 1 means a tie to break
         // on all four words.  cand: bit m = member m < 32 with |dx| in range
+        // The first kRankBatch x words are loaded together, so their
+        // latencies overlap (record-major bins put each member on its own
+        // line); larger cells continue one member at a time.
+        constexpr uint32_t kRankBatch = 8;
         uint32_t rank = 0, le = 0, cand = 0;
-        for (uint32_t m = 0; m < on; ++m) {
-          const float qx = __ldg(&cbx[4 * m]);
+        float xs[kRankBatch];
+#pragma unroll
+        for (uint32_t m = 0; m < kRankBatch; ++m) xs[m] = m < on ? cb.ldg_x(m) : 0.0f;
+#pragma unroll
+        for (uint32_t m = 0; m < kRankBatch; ++m) {
+          if (m >= on) break;
+          const uint32_t qb = __float_as_uint(xs[m]);
+          rank += qb < rx ? 1u : 0u;
+          le += qb <= rx ? 1u : 0u;
+          if (fabsf(__fsub_rn(xs[m], ra.x)) <= xlim) cand |= 1u << m;
+        }
+        for (uint32_t m = kRankBatch; m < on; ++m) {
+          const float qx = cb.ldg_x(m);
           const uint32_t qb = __float_as_uint(qx);
           rank += qb < rx ? 1u : 0u;
           le += qb <= rx ? 1u : 0u;
@@ -951,12 +991,12 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
           while (cand) {
             const uint32_t m = (uint32_t)(__ffs(cand) - 1);
             cand &= cand - 1u;
-            const float4 qm = __ldg(&cb[m]);
+            const float4 qm = cb.ldg(m);
             const int32_t bb = pair_reaction(p, k, qm);
             if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
           }
           for (uint32_t m = max(j + 1u, 32u); m < on; ++m) {  // cells of 33..kBigCell records
-            const float4 qm = __ldg(&cb[m]);
+            const float4 qm = cb.ldg(m);
             const int32_t bb = pair_reaction(p, k, qm);
             if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
           }
@@ -1060,7 +1100,7 @@ __global__ void __launch_bounds__(256) k_pairs_big_sort(KParams p) {
       if (threadIdx.x == 0) atomicOr(&c->status, kStatBounds);
       continue;  // uniform over the CTA
     }
-    const float4* __restrict__ cb = cell_records<kBinned>(p, cell, cs);
+    const CellView cb = cell_records<kBinned>(p, cell, cs);
     float4* out = nx + cs;
     float4* tmp = p.big_scratch + cs;
     for (uint32_t c0 = 0; c0 < n; c0 += kBigChunk) {
@@ -1222,9 +1262,9 @@ __global__ void __launch_bounds__(256) k_pairs_big_pairs(KParams p) {
               if (forward) sweep_sorted<false>(p, c, k, ca, p.big_scratch + ns, nn, ns, -1);
               continue;  // a large lower-key neighbour finds this pair itself
             }
-            const float4* __restrict__ nb = cell_records<kBinned>(p, nkey, ns);
+            const CellView nb = cell_records<kBinned>(p, nkey, ns);
             for (uint32_t m = 0; m < nn; ++m) {
-              const float4 q = __ldg(&nb[m]);
+              const float4 q = nb.ldg(m);
               const int32_t b = pair_reaction(p, k, q);
               if (b >= 0) emit<false>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
             }
