@@ -836,7 +836,21 @@ __device__ __forceinline__ void visit_neighbour(const KParams& p, DevCtrl* c, co
   const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
   if (nn > kBigCell) return;  // pairs with large cells are found by k_pairs_big_pairs
   const CellView nb = cell_records<kBinned>(p, nkey, ns);
-  for (uint32_t m = 0; m < nn; ++m) {
+  // x words of the first members together (overlapping latencies); a full
+  // record only for members within the x window
+  constexpr uint32_t kBatch = 8;
+  float xs[kBatch];
+#pragma unroll
+  for (uint32_t m = 0; m < kBatch; ++m) xs[m] = m < nn ? nb.ldg_x(m) : 0.0f;
+#pragma unroll
+  for (uint32_t m = 0; m < kBatch; ++m) {
+    if (m >= nn) break;
+    if (fabsf(__fsub_rn(xs[m], k.r.x)) > k.xlim) continue;
+    const float4 q = nb.ldg(m);
+    const int32_t b = pair_reaction(p, k, q);
+    if (b >= 0) emit<kSingle>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
+  }
+  for (uint32_t m = kBatch; m < nn; ++m) {
     const float4 q = nb.ldg(m);
     const int32_t b = pair_reaction(p, k, q);
     if (b >= 0) emit<kSingle>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
