@@ -181,8 +181,7 @@ def algorithmic_bytes(kernel, n_in, n_out, n_cells, binned=True):
     table = {
         "k_bin": 16 * n_in + 16 * n_out + 4 * n_cells,      # read records, write bins, histogram
         "k_count": 16 * n_in + 4 * n_cells,                 # read records, write histogram
-        "k_scan_tiles": 4 * n_cells,
-        "k_scan_down": 8 * n_cells,                          # read counts, write starts
+        "k_scan": 8 * n_cells,                               # read counts, write starts
         "k_scatter": 16 * n_in + 16 * n_out + 8 * n_cells,   # read + write records, starts + counts
         # read + write records, starts (+ clear the bin counts)
         "k_pairs_cells": 32 * n_out + (8 if binned else 4) * n_cells,

@@ -127,6 +127,7 @@ struct bd_system {
   DevBuf<unsigned long long> events, pending;
   DevBuf<float4> state0, state1, scatter, bins;
   DevBuf<uint32_t> best, cell_count, cell_start, tile_sums, big;
+  DevBuf<unsigned long long> scan_flags;
   DevBuf<float4> big_scratch;  // allocated when a cell first outgrows the pair kernel
   DevBuf<DevPair> pairs;
 
@@ -199,6 +200,7 @@ KParams make_params(bd_system* h) {
   p.cell_count = h->cell_count.p;
   p.cell_start = h->cell_start.p;
   p.tile_sums = h->tile_sums.p;
+  p.scan_flags = h->scan_flags.p;
   p.pairs = h->pairs.p;
   p.best = h->best.p;
   p.events = h->events.p;
@@ -489,6 +491,8 @@ bd_status layout_cells(bd_system* h) {
   BD_CUDA(ensure(h->cell_start, (size_t)h->n_cells + 1));
   BD_CUDA(cudaMemsetAsync(h->cell_start.p, 0, ((size_t)h->n_cells + 1) * sizeof(uint32_t), h->stream));
   BD_CUDA(ensure(h->tile_sums, (size_t)std::max<uint32_t>(h->n_tiles, 1)));
+  BD_CUDA(ensure(h->scan_flags, (size_t)std::max<uint32_t>(h->n_tiles, 1)));
+  BD_CUDA(cudaMemsetAsync(h->scan_flags.p, 0, h->scan_flags.n * sizeof(unsigned long long), h->stream));
   BD_CUDA(cudaStreamSynchronize(h->stream));
   if (!h->panels.empty()) {
     const bd_status st = upload_cell_masks(h);
@@ -705,6 +709,7 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->cell_count.free();
   h->cell_start.free();
   h->tile_sums.free();
+  h->scan_flags.free();
   h->pairs.free();
   h->dpanels.free();
   h->dsurf_act.free();
@@ -1222,10 +1227,12 @@ BD_API bd_status bd_synchronize(bd_handle h) {
       }
       BD_CUDA(cudaMemsetAsync(h->cell_count.p, 0, (size_t)h->n_cells * sizeof(uint32_t), h->stream));
       BD_CUDA(cudaMemsetAsync(h->pending.p, 0, h->pending.n * sizeof(unsigned long long), h->stream));
+      BD_CUDA(cudaMemsetAsync(h->scan_flags.p, 0, h->scan_flags.n * sizeof(unsigned long long), h->stream));
       c.status = 0;
       c.n_pairs = 0;
       c.n_big = 0;
       c.n_surf = 0;
+      c.scan_ticket = 0;
       c.n_virtual = 0;
       st = push_ctrl(h);
       if (st) return st;
@@ -1790,7 +1797,7 @@ BD_API const char* bd_stage_name(bd_handle h, int k) {
 BD_API bd_status bd_get_kernels_per_step(bd_handle h, int* n) {
   if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
   if (h->diffuse_only()) *n = (h->Z > 0 ? 2 : 0) + 2;
-  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 7 : 8) + (h->B > 0 ? 1 : 0) + (h->binned && !h->panels.empty() ? 1 : 0);
+  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 5 : 6) + (h->B > 0 ? 1 : 0) + (h->binned && !h->panels.empty() ? 1 : 0);
   return BD_OK;
 }
 

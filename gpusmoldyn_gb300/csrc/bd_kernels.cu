@@ -410,60 +410,119 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
   });
 }
 
-__global__ void __launch_bounds__(1024) k_scan_tiles(KParams p) {
-  __shared__ uint32_t s_total;
-  if (ld_u32(&p.ctrl->status)) return;
-  const uint32_t base = blockIdx.x * kScanTile;
-  uint32_t sum = 0;
-#pragma unroll
-  for (uint32_t k = 0; k < kScanTile / 1024; ++k) {
-    const uint32_t idx = base + k * 1024 + threadIdx.x;
-    if (idx < p.n_cells) sum += ld_u32(&p.cell_count[idx]);
-  }
-  block_exclusive_scan<1024>(sum, &s_total);
-  if (threadIdx.x == 0) p.tile_sums[blockIdx.x] = s_total;
+// Single-pass exclusive scan of the cell counts into cell_start, by
+// decoupled look-back (D. Merrill
+// and M. Garland, "Single-pass parallel prefix scan with decoupled
+// look-back", NVIDIA NVR-2016-002).  Each CTA takes the next tile by an
+// atomic ticket, so a tile only ever waits on tiles that CTAs already
+// running have taken; it publishes its sum (kScanAggregate), adds the
+// sums published before it, walking back until a tile that knows its full
+// prefix (kScanInclusive), and publishes that.  The first warp does the
+// walk, 32 predecessors per poll, with at most kScanPolls polls that find a
+// flag not yet written, after which the step stops with kStatTimeout.  The flags and the ticket are cleared when
+// the step commits (k_match) and by the host before a replay.
+constexpr unsigned long long kScanAggregate = 1ull << 32, kScanInclusive = 2ull << 32;
+constexpr uint32_t kScanPolls = 1u << 20;
+
+__device__ __forceinline__ void store_release(unsigned long long* a, unsigned long long v) {
+  asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long load_acquire(const unsigned long long* a) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+  return v;
 }
 
-__global__ void __launch_bounds__(1024) k_scan_top(KParams p) {
-  __shared__ uint32_t s_total;
+__global__ void __launch_bounds__(1024) k_scan(KParams p) {
+  __shared__ uint32_t s_tile, s_total, s_prefix, s_stop;
   DevCtrl* c = p.ctrl;
-  if (ld_u32(&c->status)) return;
-  uint32_t carry = 0;
-  for (uint32_t base = 0; base < p.n_tiles; base += 1024) {
-    const uint32_t t = base + threadIdx.x;
-    const uint32_t v = t < p.n_tiles ? p.tile_sums[t] : 0u;
-    const uint32_t ex = block_exclusive_scan<1024>(v, &s_total);
-    const uint32_t tot = s_total;
-    if (t < p.n_tiles) p.tile_sums[t] = carry + ex;
-    carry += tot;
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {
-    c->n_sorted = carry;
-    if (carry > p.capacity) atomicOr(&c->status, kStatCapacity);
+    s_stop = ld_u32(&c->status) != 0u;
+    if (!s_stop) s_tile = atomicAdd(&c->scan_ticket, 1u);
   }
-}
-
-__global__ void __launch_bounds__(1024) k_scan_down(KParams p) {
-  __shared__ uint32_t s_total;
-  DevCtrl* c = p.ctrl;
-  if (ld_u32(&c->status)) return;
-  constexpr uint32_t kPer = kScanTile / 1024;
-  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kPer;
+  __syncthreads();
+  if (s_stop || s_tile >= p.n_tiles) return;  // uniform over the CTA
+  const uint32_t tile = s_tile;
+  constexpr uint32_t kPer = kScanTile / 1024;  // consecutive counts per thread, 16-byte aligned
+  static_assert(kPer % 4 == 0, "vector loads of 4 counts");
+  const uint32_t base = tile * kScanTile + threadIdx.x * kPer;
+  const bool whole = base + kPer <= p.n_cells;
   uint32_t v[kPer];
   uint32_t sum = 0;
 #pragma unroll
-  for (uint32_t k = 0; k < kPer; ++k) {
-    v[k] = (base + k < p.n_cells) ? ld_u32(&p.cell_count[base + k]) : 0u;
-    sum += v[k];
+  for (uint32_t k = 0; k < kPer; k += 4) {
+    if (whole) {
+      const uint4 q = __ldcg(reinterpret_cast<const uint4*>(p.cell_count + base + k));
+      v[k] = q.x, v[k + 1] = q.y, v[k + 2] = q.z, v[k + 3] = q.w;
+    } else {
+#pragma unroll
+      for (uint32_t e = 0; e < 4; ++e) v[k + e] = base + k + e < p.n_cells ? ld_u32(&p.cell_count[base + k + e]) : 0u;
+    }
   }
-  uint32_t run = p.tile_sums[blockIdx.x] + block_exclusive_scan<1024>(sum, &s_total);
+#pragma unroll
+  for (uint32_t k = 0; k < kPer; ++k) sum += v[k];
+  const uint32_t excl = block_exclusive_scan<1024>(sum, &s_total);
+  if (threadIdx.x < 32) {
+    // the look-back, one warp: lane l reads the flag of tile pred - l, so a
+    // poll resolves up to 32 predecessors
+    const uint32_t lane = threadIdx.x, agg = s_total;
+    uint32_t prefix = 0;
+    if (tile > 0) {
+      if (lane == 0) store_release(&p.scan_flags[tile], kScanAggregate | agg);
+      int32_t pred = (int32_t)tile - 1;
+      uint32_t polls = 0;
+      for (;;) {
+        const int32_t t = pred - (int32_t)lane;
+        // before tile 0 there is nothing: an inclusive sum of 0
+        const unsigned long long f = t >= 0 ? load_acquire(&p.scan_flags[t]) : kScanInclusive;
+        const uint32_t inc = __ballot_sync(kFull, (f & kScanInclusive) != 0ull);
+        const uint32_t ready = __ballot_sync(kFull, f != 0ull);
+        const uint32_t upto = inc ? (uint32_t)(__ffs(inc) - 1) : 31u;  // nearest inclusive flag
+        const uint32_t need = upto == 31u ? kFull : ((2u << upto) - 1u);
+        if ((ready & need) == need) {
+          uint32_t v = lane <= upto ? (uint32_t)f : 0u;
+#pragma unroll
+          for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+          prefix += v;
+          if (inc) break;
+          pred -= 32;
+          continue;
+        }
+        if (++polls > kScanPolls) {
+          if (lane == 0) atomicOr(&c->status, kStatTimeout);
+          break;
+        }
+      }
+    }
+    if (lane == 0) {
+      store_release(&p.scan_flags[tile], kScanInclusive | (prefix + agg));
+      s_prefix = prefix;
+      if (tile == p.n_tiles - 1) {
+        const uint32_t total = prefix + agg;
+        p.cell_start[p.n_cells] = total;
+        c->n_sorted = total;
+        if (total > p.capacity) atomicOr(&c->status, kStatCapacity);
+      }
+    }
+  }
+  __syncthreads();
+  uint32_t run = s_prefix + excl;
 #pragma unroll
   for (uint32_t k = 0; k < kPer; ++k) {
-    if (base + k < p.n_cells) p.cell_start[base + k] = run;
-    run += v[k];
+    const uint32_t x = v[k];
+    v[k] = run;
+    run += x;
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) p.cell_start[p.n_cells] = ld_u32(&c->n_sorted);
+#pragma unroll
+  for (uint32_t k = 0; k < kPer; k += 4) {
+    if (whole) {
+      *reinterpret_cast<uint4*>(p.cell_start + base + k) = make_uint4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+    } else {
+#pragma unroll
+      for (uint32_t e = 0; e < 4; ++e)
+        if (base + k + e < p.n_cells) p.cell_start[base + k + e] = v[k + e];
+    }
+  }
 }
 
 template <bool kTable, int kMinBlocks, bool kSingle, int kSurf = 0>
@@ -1419,6 +1478,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     atomicExch(&p.best[pr[k].j], kFree);
   }
   commit_events(p);
+  for (uint32_t t = threadIdx.x; t < p.n_tiles; t += blockDim.x) p.scan_flags[t] = 0ull;
   for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) {
     const DevInstance& I = p.inst[inst];
     advance_instance_step(p, inst, step_now);
@@ -1429,6 +1489,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     c->n_pairs = 0;
     c->n_big = 0;
     c->n_surf = 0;
+    c->scan_ticket = 0;
     c->deaths_last = s_deaths;
     c->n_slots = c->n_sorted;
     c->n_virtual = 0;
@@ -1604,12 +1665,8 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
       BD_STREAM_LAUNCH(k_bin, 0);
       done("k_bin");
     }
-    k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
-    done("k_scan_tiles");
-    k_scan_top<<<1, 1024, 0, s>>>(p);
-    done("k_scan_top");
-    k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
-    done("k_scan_down");
+    k_scan<<<p.n_tiles, 1024, 0, s>>>(p);
+    done("k_scan");
     BD_PAIRS_LAUNCH(true);
     done("k_pairs_cells");
     k_pairs_big_sort<true><<<kBigGrid, 256, 0, s>>>(p);
@@ -1625,12 +1682,8 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   }
   BD_STREAM_LAUNCH_COMPACT(k_count);
   done("k_count");
-  k_scan_tiles<<<p.n_tiles, 1024, 0, s>>>(p);
-  done("k_scan_tiles");
-  k_scan_top<<<1, 1024, 0, s>>>(p);
-  done("k_scan_top");
-  k_scan_down<<<p.n_tiles, 1024, 0, s>>>(p);
-  done("k_scan_down");
+  k_scan<<<p.n_tiles, 1024, 0, s>>>(p);
+  done("k_scan");
   BD_STREAM_LAUNCH_COMPACT(k_scatter);
   done("k_scatter");
   BD_PAIRS_LAUNCH(false);

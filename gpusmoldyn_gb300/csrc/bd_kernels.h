@@ -31,6 +31,7 @@ struct KParams {
   uint32_t* cell_count;       // [n_cells] particles per cell (returns to 0 each step)
   uint32_t* cell_start;       // [n_cells + 1] exclusive prefix of cell_count
   uint32_t* tile_sums;        // [n_tiles] scan partials
+  unsigned long long* scan_flags; // [n_tiles] single-pass scan: state << 32 | sum, 0 between steps
   DevPair* pairs;             // [pair_cap]
   uint32_t* best;             // [capacity] matcher scratch, all 0xFFFFFFFF between steps
   unsigned long long* events; // [I * R] reaction event counters (committed steps)
@@ -83,6 +84,6 @@ void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaS
 void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaStream_t stream);
 
 // Tile size of the cell scan.
-constexpr uint32_t kScanTile = 4096;
+constexpr uint32_t kScanTile = 16384;
 
 }  // namespace bd

@@ -111,7 +111,8 @@ struct DevCtrl {
   uint32_t bin_need;       // largest cell occupancy seen by a bin that overflowed
   uint32_t n_big;          // cells queued for the large-cell pair kernel
   uint32_t n_surf;         // records whose move meets a panel box (binned path with surfaces)
-  uint32_t pad[2];
+  uint32_t scan_ticket;    // tiles taken by the single-pass cell scan of the step in flight
+  uint32_t pad[1];
 };
 
 enum StatusBits : uint32_t {
