@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(1024) k_scan(KParams p) {
       }
     }
     if (lane == 0) {
-      store_release(&p.scan_flags[tile], kScanInclusive | (prefix + agg));
+      if (!(p.scan_withhold && tile == 0)) store_release(&p.scan_flags[tile], kScanInclusive | (prefix + agg));
       s_prefix = prefix;
       if (tile == p.n_tiles - 1) {
         const uint32_t total = prefix + agg;
@@ -693,6 +693,12 @@ __global__ void __launch_bounds__(256, 2) k_bin_surface(KParams p) {
   const float4* __restrict__ st = cur_state(p, ld_u32(&c->cur));
   const uint32_t n = min(ld_u32(&c->n_surf), p.capacity);
   const uint32_t stride = gridDim.x * blockDim.x;
+  // first products keep k_bin's deferred claim (consumed one record later)
+  PendingClaim pending;
+  pending.key = kNoKey;
+  pending.old = 0;
+  pending.leader = 0;
+  pending.rank = 0;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {  // CTA-uniform trip count
     const uint32_t e = base + threadIdx.x;
     Out2 o;
@@ -701,9 +707,12 @@ __global__ void __launch_bounds__(256, 2) k_bin_surface(KParams p) {
       const uint32_t i = p.surf_queue[e];
       advance_rec<kTable, true, kSingle, 1>(p, ctx, st[i], i, o);
     }
-    claim_retire(p, c, claim_issue(p.cell_count, o.n > 0 ? o.key[0] : kNoKey, o.r[0]));
+    const PendingClaim next = claim_issue(p.cell_count, o.n > 0 ? o.key[0] : kNoKey, o.r[0]);
     if (__any_sync(kFull, o.n > 1)) claim_retire(p, c, claim_issue(p.cell_count, o.n > 1 ? o.key[1] : kNoKey, o.r[1]));
+    claim_retire(p, c, pending);
+    pending = next;
   }
+  claim_retire(p, c, pending);
 }
 
 // The records of one cell, m-th at base[m * stride]: a bin of the binned

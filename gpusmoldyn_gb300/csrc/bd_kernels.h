@@ -32,6 +32,7 @@ struct KParams {
   uint32_t* cell_start;       // [n_cells + 1] exclusive prefix of cell_count
   uint32_t* tile_sums;        // [n_tiles] scan partials
   unsigned long long* scan_flags; // [n_tiles] single-pass scan: state << 32 | sum, 0 between steps
+  uint32_t scan_withhold;     // test switch: tile 0 of the scan does not publish (its successors time out)
   DevPair* pairs;             // [pair_cap]
   uint32_t* best;             // [capacity] matcher scratch, all 0xFFFFFFFF between steps
   unsigned long long* events; // [I * R] reaction event counters (committed steps)

@@ -253,6 +253,11 @@ BD_API bd_status bd_get_stage_times(bd_handle h, float *ms, int n);
 BD_API bd_status bd_debug_get_slots(bd_handle h, float *xyz4, uint32_t *w, size_t cap, size_t *n);
 /* Cell start offsets of the last sorted step (ncells + 1 entries). */
 BD_API bd_status bd_debug_get_cells(bd_handle h, uint32_t *start, size_t cap, size_t *ncells);
+/* Test switch for the bounded wait of the single-pass cell scan: with on,
+ * the scan's first tile keeps its sum to itself, so the next tile's wait
+ * for it runs out (after about a second) and the step reports
+ * BD_ERR_TIMEOUT instead of hanging.  No fault, trap or endless loop. */
+BD_API bd_status bd_debug_withhold_scan(bd_handle h, int on);
 /* Candidate pairs (slot_i, slot_j, reaction, accepted) of the last step. */
 BD_API bd_status bd_debug_get_pairs(bd_handle h, uint32_t *quads, size_t cap, size_t *n);
 /* Uniform-grid geometry of one instance: cells per axis, cell edge lengths
