@@ -511,7 +511,7 @@ bd_status layout_cells(bd_system* h) {
     if (k < (int)h->plan_n.size()) lam = std::max(lam, (double)h->plan_n[k] / cells);
   }
   uint32_t K = (uint32_t)ceil(lam + 7.0 * sqrt(lam) + 8.0);
-  K = std::max<uint32_t>((K + 3u) & ~3u, h->bin_cap);
+  K = std::max<uint32_t>((K + kBinGroup - 1) / kBinGroup * kBinGroup, h->bin_cap);
   const uint64_t bytes = (uint64_t)h->n_cells * K * sizeof(float4);
   const uint32_t mode = h->cfg.sort_mode;
   h->binned = mode == BD_SORT_BINNED || (mode == BD_SORT_AUTO && bytes <= kBinBudgetBytes);
@@ -1209,7 +1209,7 @@ BD_API bd_status bd_synchronize(bd_handle h) {
         // a cell outgrew its bin: larger bins, or the compact sort when
         // they would not fit the automatic budget
         uint64_t K = std::max<uint64_t>((uint64_t)c.bin_need + c.bin_need / 4 + 4, (uint64_t)h->bin_cap + 8);
-        K = (K + 3) & ~3ull;
+        K = (K + kBinGroup - 1) / kBinGroup * kBinGroup;
         const bool fits = (uint64_t)h->n_cells * K * sizeof(float4) <= kBinBudgetBytes;
         if (K > 0xFFFFFFF0ull || (!fits && h->cfg.sort_mode != BD_SORT_BINNED)) {
           h->binned = false;

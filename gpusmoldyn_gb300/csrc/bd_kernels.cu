@@ -556,16 +556,16 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_scatter(KParams p) {
   });
 }
 
-// Bin layout.  Record-major: place `off` of every cell is one contiguous
-// array, bins[off * n_cells + cell].  The records a warp bins belong to a
-// few consecutive cells (the state is in cell order), so their stores, and
-// the pair kernel's loads of the same place across 32 consecutive cells,
-// fall on a few contiguous lines; cell-major bins (bins[cell * bin_cap +
-// off]) put each cell on its own line.
-constexpr bool kBinRecordMajor = true;
-
+// Bin layout.  A cell's places come in groups of kBinGroup, stored
+// together, and group g of every cell forms one contiguous array:
+// place off of a cell is bins[(g * n_cells + cell) * kBinGroup + off %
+// kBinGroup], g = off / kBinGroup.  The records a warp bins belong to a
+// few consecutive cells (the state is in cell order), so their stores fall
+// on a few contiguous lines, and a cell's first records fill whole 32-byte
+// sectors rather than half of one shared with a neighbour cell.  The pair
+// kernel reads a cell's first kBinGroup places from one group.
 __device__ __forceinline__ size_t bin_index(const KParams& p, uint32_t cell, uint32_t off) {
-  return kBinRecordMajor ? (size_t)off * p.n_cells + cell : (size_t)cell * p.bin_cap + off;
+  return ((size_t)(off / kBinGroup) * p.n_cells + cell) * kBinGroup + off % kBinGroup;
 }
 
 // A record waiting for its place in a bin: the warp's claim (atomicAdd on
@@ -683,7 +683,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
 // their move meets a panel box, advanced with the surface walk (the same
 // Philox counters, so the same step) and put into their bins.
 template <bool kTable, bool kSingle>
-__global__ void __launch_bounds__(256, 2) k_bin_surface(KParams p) {
+__global__ void __launch_bounds__(256, 4) k_bin_surface(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
   __shared__ DevUni s_uni[kSingle ? kCtxUni : 1];
   SingleCtx ctx{};
@@ -715,16 +715,18 @@ __global__ void __launch_bounds__(256, 2) k_bin_surface(KParams p) {
   claim_retire(p, c, pending);
 }
 
-// The records of one cell, m-th at base[m * stride]: a bin of the binned
-// sort (record-major bins: stride = the number of cells) or a range of the
-// compact scatter buffer (stride 1).
+// The records of one cell, m-th at base[(m / kBinGroup) * stride + m %
+// kBinGroup]: a bin of the binned sort (stride = kBinGroup x the number of
+// cells) or a range of the compact scatter buffer (stride kBinGroup, so
+// the m-th record is base[m]).
 struct CellView {
   const float4* base;
   size_t stride;
-  __device__ __forceinline__ float4 operator[](uint32_t m) const { return base[(size_t)m * stride]; }
-  __device__ __forceinline__ float4 ldg(uint32_t m) const { return __ldg(base + (size_t)m * stride); }
+  __device__ __forceinline__ size_t at(uint32_t m) const { return (size_t)(m / kBinGroup) * stride + m % kBinGroup; }
+  __device__ __forceinline__ float4 operator[](uint32_t m) const { return base[at(m)]; }
+  __device__ __forceinline__ float4 ldg(uint32_t m) const { return __ldg(base + at(m)); }
   __device__ __forceinline__ float ldg_x(uint32_t m) const {
-    return __ldg(reinterpret_cast<const float*>(base + (size_t)m * stride));
+    return __ldg(reinterpret_cast<const float*>(base + at(m)));
   }
 };
 
@@ -768,8 +770,8 @@ constexpr int kBigGrid = 304;  // CTAs of the large-cell kernels (cells they tak
 // First record of a cell: its bin, or its range of the compact scatter buffer.
 template <bool kBinned>
 __device__ __forceinline__ CellView cell_records(const KParams& p, uint32_t cell, uint32_t cs) {
-  if (kBinned) return CellView{p.bins + bin_index(p, cell, 0), kBinRecordMajor ? (size_t)p.n_cells : 1u};
-  return CellView{p.scatter + cs, 1u};
+  if (kBinned) return CellView{p.bins + bin_index(p, cell, 0), (size_t)p.n_cells * kBinGroup};
+  return CellView{p.scatter + cs, kBinGroup};
 }
 
 // A record looking for partners.
@@ -1042,8 +1044,8 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
         // record itself among them), so le - rank > 1 means a tie to break
         // on all four words.  cand: bit m = member m < 32 with |dx| in range
         // The first kRankBatch x words are loaded together, so their
-        // latencies overlap (record-major bins put each member on its own
-        // line); larger cells continue one member at a time.
+        // latencies overlap (each group of kBinGroup members lies on its
+        // own line); larger cells continue one member at a time.
         constexpr uint32_t kRankBatch = 8;
         uint32_t rank = 0, le = 0, cand = 0;
         float xs[kRankBatch];

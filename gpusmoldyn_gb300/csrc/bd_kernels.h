@@ -87,4 +87,8 @@ void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaSt
 // Tile size of the cell scan.
 constexpr uint32_t kScanTile = 16384;
 
+// Places of a cell bin stored together (64 bytes); the bin capacity is a
+// multiple of it.
+constexpr uint32_t kBinGroup = 4;
+
 }  // namespace bd
