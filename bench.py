@@ -408,6 +408,10 @@ def run_gb300(args, dist):
         out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": f"c3 network at the c3 density: 262144 particles in a {side:.1f} um cube,"
                                          f" {done} steps ({el:.1f} s), OpenMP {threads} threads"}
+        # the same sample on one core
+        rate1, done1, el1, _ = cpu_oracle_rate(262144, 200, 1, budget_s=10.0)
+        out["cpu_baseline"]["single_core"] = {"value": rate1, "unit": UNIT, "cores": 1,
+                                              "sample": f"the same sample, {done1} steps ({el1:.1f} s), 1 thread"}
     return out
 
 
