@@ -132,7 +132,6 @@ _SIGS = {
     "bd_synchronize": (C.c_int, [H]),
     "bd_get_step": (C.c_int, [H, C.POINTER(C.c_uint64)]),
     "bd_get_event_counts": (C.c_int, [H, P, C.c_int]),
-    "bd_get_stage_times": (C.c_int, [H, P, C.c_int]),
     "bd_time_steps": (C.c_int, [H, C.c_int, C.POINTER(C.c_float)]),
     "bd_profile_steps": (C.c_int, [H, C.c_int, P, C.c_int, C.POINTER(C.c_int)]),
     "bd_stage_name": (C.c_char_p, [H, C.c_int]),

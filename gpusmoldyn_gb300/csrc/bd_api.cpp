@@ -1803,12 +1803,6 @@ BD_API bd_status bd_get_kernels_per_step(bd_handle h, int* n) {
   return BD_OK;
 }
 
-BD_API bd_status bd_get_stage_times(bd_handle h, float* ms, int n) {
-  if (!h || !ms) return BD_ERR_INVALID_ARGUMENT;
-  for (int k = 0; k < n; k++) ms[k] = 0.0f;
-  return BD_OK;
-}
-
 BD_API bd_status bd_debug_get_slots(bd_handle h, float* xyz4, uint32_t* w, size_t cap, size_t* n) {
   if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
   *n = 0;

@@ -244,9 +244,6 @@ BD_API const char *bd_stage_name(bd_handle h, int k);
 /* Kernel launches in one timestep of the current configuration. */
 BD_API bd_status bd_get_kernels_per_step(bd_handle h, int *n);
 
-/* Unused; kept for layout stability of older callers.  Zero-fills ms. */
-BD_API bd_status bd_get_stage_times(bd_handle h, float *ms, int n);
-
 /* --------------------------------------------------- parity / inspection */
 
 /* Raw slot array of the current state, holes included (w = 0xFFFFFFFF). */
