@@ -92,3 +92,40 @@ def test_ensemble_upload_assigns_instances():
     bad[5, 0] = 1.5
     with pytest.raises(L.BDError):
         s.set_ensemble_particles(bad, sp, counts)
+
+
+def test_export_into_short_and_pinned_arrays():
+    """An array shorter than the live count receives its first entries and
+    nothing past them; positions alone may be asked for; pinned arrays
+    receive the same result as pageable ones."""
+    import ctypes as C
+
+    import torch
+
+    from gpusmoldyn_gb300.system import _ptr
+
+    s, pos, sp = small(seed=53, n=20000)
+    s.set_particles(pos, sp)
+    s.step(20)
+    s.synchronize()
+    p4, q = s.particles4()
+    m = len(q) // 3
+    short = (np.full((m + 8, 4), -1, np.float32), np.full(m + 8, -1, np.int32))
+    got = C.c_size_t()
+    L.check(s.lib.bd_get_instance_particles(s.h, -1, _ptr(short[0]), _ptr(short[1]), m, C.byref(got)),
+            "bd_get_particles")
+    assert got.value == len(q)
+    np.testing.assert_array_equal(short[0][:m], p4[:m])
+    np.testing.assert_array_equal(short[1][:m], q[:m])
+    assert (short[0][m:] == -1).all() and (short[1][m:] == -1).all()
+    # positions only
+    only = np.full((len(q), 4), -1, np.float32)
+    L.check(s.lib.bd_get_instance_particles(s.h, -1, _ptr(only), None, len(q), C.byref(got)), "bd_get_particles")
+    np.testing.assert_array_equal(only, p4)
+    pin_p = torch.full((len(q) + 8, 4), -1.0, dtype=torch.float32).pin_memory()
+    pin_s = torch.full((len(q) + 8,), -1, dtype=torch.int32).pin_memory()
+    p4c, qc = s.particles4(out=(pin_p.numpy(), pin_s.numpy()))
+    np.testing.assert_array_equal(p4c, p4)
+    np.testing.assert_array_equal(qc, q)
+    assert (pin_s.numpy()[len(q):] == -1).all()
+    s.close()
