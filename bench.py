@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--no-surfaces", action="store_true")
     p.add_argument("--serve-jobs", type=int, default=40)
     p.add_argument("--profile-only", action="store_true", help="build + a few steps (for ncu)")
+    p.add_argument("--profile-surfaces", action="store_true",
+                   help="with --profile-only: the c3 step inside the cell (k_bin_surface)")
     return p.parse_args()
 
 
@@ -299,6 +301,14 @@ def run_gb300(args, dist):
     libbuild.build()
     gpusmoldyn_gb300.load()
     device = dist.local
+    if args.profile_only and args.profile_surfaces:
+        n = args.n or 16_000_000
+        s = configs.build_c3(n=n, side=200.0 * (n / 16_000_000) ** (1 / 3), surfaces=True, device=device)
+        s.step(args.warmup + 3)
+        s.synchronize()
+        print(json.dumps({"profile_only": True, "surfaces": True, "n": s.count()}))
+        s.close()
+        return None
     # ---------------- headline: device-timed plain step
     s, desc = build_workload(args.workload, args.n, device=device)
     s.step(args.warmup)
