@@ -1235,6 +1235,7 @@ BD_API bd_status bd_synchronize(bd_handle h) {
       c.n_big = 0;
       c.n_surf = 0;
       c.scan_ticket = 0;
+      c.surf_ticket = 0;
       c.n_virtual = 0;
       st = push_ctrl(h);
       if (st) return st;

@@ -681,7 +681,11 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_bin(KParams p) {
 
 // Binned path with surfaces, pass 1b: the records k_bin queued because
 // their move meets a panel box, advanced with the surface walk (the same
-// Philox counters, so the same step) and put into their bins.
+// Philox counters, so the same step) and put into their bins.  A walk's
+// cost varies with the panels near the record (one sphere against a mesh
+// of many triangles), and the queue holds neighbouring records together,
+// so warps take 32 queue entries at a time from a counter until the queue
+// is empty: a warp of slow walks does not hold the others' share.
 template <bool kTable, bool kSingle>
 __global__ void __launch_bounds__(256, 4) k_bin_surface(KParams p) {
   __shared__ DevSpecies s_species[kSingle ? kCtxSpecies : 1];
@@ -692,15 +696,19 @@ __global__ void __launch_bounds__(256, 4) k_bin_surface(KParams p) {
   if (ctrl_status_warp(c)) return;
   const float4* __restrict__ st = cur_state(p, ld_u32(&c->cur));
   const uint32_t n = min(ld_u32(&c->n_surf), p.capacity);
-  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t lane = lane_id();
   // first products keep k_bin's deferred claim (consumed one record later)
   PendingClaim pending;
   pending.key = kNoKey;
   pending.old = 0;
   pending.leader = 0;
   pending.rank = 0;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {  // CTA-uniform trip count
-    const uint32_t e = base + threadIdx.x;
+  for (;;) {  // warp-uniform trip count
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&c->surf_ticket, 32u);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= n) break;
+    const uint32_t e = base + lane;
     Out2 o;
     o.n = 0;
     if (e < n) {
@@ -1501,6 +1509,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     c->n_big = 0;
     c->n_surf = 0;
     c->scan_ticket = 0;
+    c->surf_ticket = 0;
     c->deaths_last = s_deaths;
     c->n_slots = c->n_sorted;
     c->n_virtual = 0;

@@ -112,7 +112,7 @@ struct DevCtrl {
   uint32_t n_big;          // cells queued for the large-cell pair kernel
   uint32_t n_surf;         // records whose move meets a panel box (binned path with surfaces)
   uint32_t scan_ticket;    // tiles taken by the single-pass cell scan of the step in flight
-  uint32_t pad[1];
+  uint32_t surf_ticket;    // queued records taken by k_bin_surface in the step in flight
 };
 
 enum StatusBits : uint32_t {
