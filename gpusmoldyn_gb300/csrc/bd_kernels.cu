@@ -350,6 +350,59 @@ __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
   DevCtrl* c = p.ctrl;
   if (ld_u32(&c->status)) return;
   const uint32_t nz = p.n_inst * p.Z;
+  if (nz <= 32u) {
+    // Few entries (one instance, a few reactions): a group of at least 32
+    // threads per entry counts the CDF values at or below u.  The CDF does
+    // not decrease, so that count is the smallest k with CDF(k) > u, the
+    // index the binary search below finds, and its loads are all in flight
+    // at once instead of one dependent load per halving.
+    __shared__ uint32_t s_part[32], s_cnt[32];
+    uint32_t groups = 1;
+    while (groups < nz) groups <<= 1;
+    const uint32_t G = 1024u / groups;  // threads per entry, a multiple of 32
+    const uint32_t g = threadIdx.x / G, t = threadIdx.x % G;
+    uint32_t le = 0;
+    if (g < nz) {
+      const uint32_t inst = g / p.Z, zr = g % p.Z;
+      const DevInstance& I = p.inst[inst];
+      if (advancing(p.inst_flags[inst])) {
+        const DevZero& Zr = p.zero[I.block * p.Z + zr];
+        const U4 r = philox(U4{zr, p.inst_step[inst], kTagZeroCount, 0u}, I.key_lo, I.key_hi);
+        const double u = u53_to_unit(r.x, r.y);
+        const double* cdf = p.cdf + Zr.cdf_off;
+        for (uint32_t k = t; k < Zr.cdf_len; k += G) le += cdf[k] <= u ? 1u : 0u;
+      }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) le += __shfl_xor_sync(kFull, le, d);
+    if ((threadIdx.x & 31u) == 0) s_part[threadIdx.x >> 5] = le;
+    __syncthreads();
+    if (threadIdx.x < nz) {
+      const uint32_t e = threadIdx.x, inst = e / p.Z, zr = e % p.Z;
+      const DevInstance& I = p.inst[inst];
+      uint32_t cnt = 0;
+      if (advancing(p.inst_flags[inst])) {
+        const DevZero& Zr = p.zero[I.block * p.Z + zr];
+        uint32_t below = 0;
+        for (uint32_t w = 0; w < G / 32u; ++w) below += s_part[e * (G / 32u) + w];
+        cnt = (uint32_t)Zr.kmin + min(below, Zr.cdf_len - 1u);
+        if (cnt) atomicAdd(&p.pending[(size_t)inst * p.R + Zr.rxn], (unsigned long long)cnt);
+      }
+      s_cnt[e] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t carry = 0;
+      for (uint32_t e = 0; e < nz; ++e) {
+        p.zero_off[e] = carry;
+        carry += s_cnt[e];
+      }
+      p.zero_off[nz] = carry;
+      c->n_virtual = carry;
+      if (check_append && (uint64_t)c->n_slots + carry > p.capacity) atomicOr(&c->status, kStatCapacity);
+    }
+    return;
+  }
   uint32_t carry = 0;
   for (uint32_t base = 0; base < nz; base += 1024) {
     const uint32_t e = base + threadIdx.x;
