@@ -197,6 +197,30 @@ def test_poisson_cdf_against_reference_sampler():
         assert samples.var() == pytest.approx(ref_var, rel=0.05)
 
 
+def test_poisson_inversion_by_count_equals_binary_search():
+    """The device inverts a zeroth-order CDF either by binary search for the
+    smallest k with CDF(k) > u or, with few entries, by counting the values
+    at or below u; the tables never decrease, so the two agree, here at a
+    mean as large as the c3 network's births per step."""
+    g = np.random.Generator(np.random.Philox(8))
+    for mean in (0.3, 7.5, 1.2e3, 4.0e4):
+        s = _host((1.0, 1.0, 1.0), 1.0)
+        s.add_species(1.0)
+        r = s.add_reaction(0, [], [0], mean)
+        s.finalize()
+        cdf, kmin = s.poisson_cdf(r)
+        assert np.all(np.diff(cdf) >= 0) and cdf[-1] == 1.0
+        for u in g.random(200):
+            lo, hi = 0, len(cdf) - 1
+            while lo < hi:
+                mid = (lo + hi) // 2
+                if cdf[mid] > u:
+                    hi = mid
+                else:
+                    lo = mid + 1
+            assert min(int(np.count_nonzero(cdf <= u)), len(cdf) - 1) == lo
+
+
 @pytest.mark.slow
 def test_rate_tables_regenerate():
     """The committed header is what the generator produces (irreversible table)."""
