@@ -200,8 +200,8 @@ def test_poisson_cdf_against_reference_sampler():
 def test_poisson_inversion_by_count_equals_binary_search():
     """The device inverts a zeroth-order CDF either by binary search for the
     smallest k with CDF(k) > u or, with few entries, by counting the values
-    at or below u; the tables never decrease, so the two agree, here at a
-    mean as large as the c3 network's births per step."""
+    at or below u; the tables never decrease, so the two agree, here at
+    means from 0.3 to 40,000 births per step."""
     g = np.random.Generator(np.random.Philox(8))
     for mean in (0.3, 7.5, 1.2e3, 4.0e4):
         s = _host((1.0, 1.0, 1.0), 1.0)
