@@ -124,6 +124,7 @@ _SIGS = {
     "bd_get_count": (C.c_int, [H, C.POINTER(C.c_uint64)]),
     "bd_get_particles": (C.c_int, [H, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_get_instance_particles": (C.c_int, [H, C.c_int, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "bd_instance_cancel": (C.c_int, [H, C.c_int]),
     "bd_get_instance_counts": (C.c_int, [H, P, C.c_int]),
     "bd_get_species_counts": (C.c_int, [H, C.c_int, P, C.c_int]),
     "bd_get_state_pointer": (C.c_int, [H, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)]),

@@ -1660,6 +1660,21 @@ BD_API bd_status bd_instance_harvest(bd_handle h, int k, float* xyz4, int* speci
   return BD_OK;
 }
 
+BD_API bd_status bd_instance_cancel(bd_handle h, int k) {
+  const Range range("bd_instance_cancel");
+  if (!h || !h->server || k < 0 || k >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->slot_used[k] || h->slot_free_after[k] != UINT64_MAX) return BD_ERR_INVALID_ARGUMENT;
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  // the device may have frozen it meanwhile: start from its flags there
+  uint32_t f = 0;
+  BD_CUDA(cudaMemcpy(&f, h->inst_flags.p + k, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  h->h_flags[k] = f | kInstRemoved;
+  if ((st = put1(h->inst_flags, k, h->h_flags[k], h->stream))) return st;
+  h->slot_free_after[k] = h->hctrl->step;
+  return BD_OK;
+}
+
 BD_API bd_status bd_get_instance_counts(bd_handle h, uint64_t* counts, int n_instances) {
   if (!h || !counts || n_instances != h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
   if (!h->have_particles) {

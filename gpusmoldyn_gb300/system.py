@@ -372,6 +372,10 @@ class System:
         m = min(n.value, cap)
         return np.ascontiguousarray(pos[:m, :3]), sp[:m]
 
+    def cancel(self, slot):
+        """Drop an admitted instance, frozen or running (bd_instance_cancel)."""
+        L.check(self.lib.bd_instance_cancel(self.h, slot), "bd_instance_cancel")
+
     def instance_state(self, slot):
         s, f = C.c_uint32(), C.c_uint32()
         L.check(self.lib.bd_instance_state(self.h, slot, C.byref(s), C.byref(f)), "bd_instance_state")

@@ -331,6 +331,11 @@ BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc *d, const
                                    size_t n, uint32_t steps, int *slot);
 BD_API bd_status bd_instance_poll(bd_handle h, int *slots, int cap, int *n_finished);
 BD_API bd_status bd_instance_harvest(bd_handle h, int slot, float *xyz4, int *species, size_t cap, size_t *n);
+/* Drops an admitted instance, frozen or still running (a cancelled
+ * request): it takes no further step, its records are gone after the next
+ * step, and its slot is free for bd_instance_admit from then on.  The other
+ * instances are not affected. */
+BD_API bd_status bd_instance_cancel(bd_handle h, int slot);
 /* Steps taken by the instance in a slot and its flags (1 active, 2 frozen). */
 BD_API bd_status bd_instance_state(bd_handle h, int slot, uint32_t *steps, uint32_t *flags);
 

@@ -122,3 +122,50 @@ def test_harvest_after_frozen_steps_equals_harvest_at_the_freeze():
         np.testing.assert_array_equal(pos, results[0][0])
         np.testing.assert_array_equal(sp, results[0][1])
     assert len(results[0][1]) > 1000
+
+
+def test_cancel_mid_flight_leaves_the_others_unchanged():
+    """A request cancelled while it runs takes no further step and its
+    records are gone after the next one; the other instances still evolve
+    bit for bit as alone, the cancelled slot is never polled, and the next
+    admission takes it."""
+    alone = {}
+    for k in (0, 2):
+        s = System(dt=1e-3, instances=1)
+        network(s)
+        desc, pos, sp, steps = job(k)
+        slot = s.admit(desc, pos, sp, steps)
+        alone[k] = run_until_frozen(s, slot)
+        s.close()
+    mix = System(dt=1e-3, instances=3)
+    network(mix)
+    slots = {}
+    for k in (0, 1, 2):
+        desc, pos, sp, steps = job(k)
+        slots[k] = mix.admit(desc, pos, sp, steps)
+    mix.step(10)
+    mix.synchronize()
+    assert mix.instance_counts()[slots[1]] > 0
+    mix.cancel(slots[1])
+    with pytest.raises(L.BDError) as e:
+        mix.cancel(slots[1])
+    assert e.value.code == L.BD_ERR_INVALID_ARGUMENT
+    mix.step(1)
+    mix.synchronize()
+    assert mix.instance_counts()[slots[1]] == 0
+    # the only free slot is the cancelled one
+    desc, pos, sp, _ = job(3)
+    new = mix.admit(desc, pos, sp, 5)
+    assert new == slots[1]
+    results, pending = {}, {slots[0]: 0, slots[2]: 2, new: 3}
+    while pending:
+        for slot in mix.poll():
+            assert slot in pending
+            results[pending.pop(slot)] = mix.harvest(slot)
+        mix.step(3)
+        mix.synchronize()
+    mix.close()
+    assert len(results[3][0]) > 0
+    for k in (0, 2):
+        np.testing.assert_array_equal(alone[k][0], results[k][0], err_msg=f"job {k}")
+        np.testing.assert_array_equal(alone[k][1], results[k][1], err_msg=f"job {k}")
