@@ -17,7 +17,9 @@ pipeline per step and the same instances stepped one by one as plain systems.
 
 --impl reference times the CPU restatement of the reference's step (the
 reference has no CPU step of its own and its CUDA 2.x code does not build
-with CUDA 13) on the host cores, on a bounded sample of the same workload.
+with CUDA 13) on all host cores, on the headline workload itself; its
+inputs are derived by oracle.params, so that arm never loads the GPU
+library.
 
 Multi-GPU (--gpus N under torchrun): instances are independent, so each
 rank advances its own replica of the workload on its own GPU; the ranks only
@@ -165,17 +167,17 @@ def measured_peak():
 
 
 def traffic_from_profiles(kernel, workload):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.startswith("dram_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+    """DRAM bytes per launch of `kernel` and where the figure comes from, read
+    from the data file beside the committed ncu summaries (None when the
+    kernel was not captured)."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json")))
+        e = d[workload][kernel]
+    except (OSError, KeyError, ValueError):
+        return None, None
+    src = (f"ncu capture at {e['capture_particles']} particles scaled x{e['scale']} to the workload "
+           f"(profiles/{e['summary']})")
+    return float(e["bytes_per_launch"]), src
 
 
 def algorithmic_bytes(kernel, n_in, n_out, n_cells, binned=True):
@@ -234,58 +236,68 @@ def network_and_particles(name, n_override, device):
     return s, pos, sp
 
 
-def c3_sample_system(n, host_only=True, seed=3):
-    """The c3 network at the c3 density in a smaller cube."""
+def oracle_c3(n, threads, seed=3):
+    """The c3 workload at n particles (c3 density) for the CPU oracle: its
+    inputs (grid, probabilities, radii, Poisson CDFs) are derived by
+    oracle.params from the network description, so libgpusmoldyn.so is never
+    loaded.  Returns the oracle, the initial records and the cube side."""
     from gpusmoldyn_gb300 import configs
+    from oracle import params as oparams
+    from oracle import py as orc
 
-    side = (n / 2.0) ** (1 / 3)
-    return configs.build_c3(n=n, side=side, seed=seed, device=-1 if host_only else 0), side
+    side = 200.0 * (n / 16_000_000) ** (1 / 3)
+    D, rx, _ = configs.c3_reactions(n / side ** 3)
+    reactions = [oparams.Reaction(order, rc, pr, k) for order, rc, pr, k in rx]
+    o = orc.OracleSystem.from_network(D, reactions, (0.0, 0.0, 0.0), (side, side, side), 1e-3, seed, n,
+                                      normal_mode=0, threads=threads)
+    pos, sp = configs.c3_particles(n, side, seed)
+    return o, orc.records(pos, sp), side
 
 
 def cpu_oracle_rate(n, steps, threads, budget_s=None, warmup=1):
-    """Particle-steps/s of the CPU restatement on a c3-network sample."""
+    """Particle-steps/s of the CPU restatement on the c3 workload at n
+    particles: `warmup` untimed steps, then up to `steps` timed ones (fewer
+    when `budget_s` runs out)."""
     import numpy as np
 
-    from oracle import py as orc
-
-    s, side = c3_sample_system(n)
-    o = orc.OracleSystem(s, threads=threads)
-    from gpusmoldyn_gb300 import configs
-
-    pos, sp = configs.c3_particles(n, side)
-    recs = orc.records(pos, sp)
-    for t in range(max(warmup, 1)):
-        recs = o.step(t, recs)["recs"]
+    o, recs, side = oracle_c3(n, threads)
+    cap = n + n // 8 + 65536
+    for t in range(warmup):
+        recs = o.step(t, recs, cap=cap)["recs"]
     done = 0
     psteps = 0
     t0 = time.perf_counter()
-    for t in range(max(warmup, 1), max(warmup, 1) + steps):
+    for t in range(warmup, warmup + steps):
         live = int(np.sum(recs[:, 3] != 0xFFFFFFFF))
-        recs = o.step(t, recs)["recs"]
+        recs = o.step(t, recs, cap=cap)["recs"]
         psteps += live
         done += 1
         if budget_s and time.perf_counter() - t0 > budget_s:
             break
     el = time.perf_counter() - t0
-    s.close()
     return psteps / el, done, el, side
 
 
 def run_reference(args, dist):
+    """The reference's step on the host cores: the oracle (the reference has
+    no CPU step and its CUDA 2.x code does not build), all host threads, on
+    the headline workload itself -- every step is a full step of the c3
+    configuration."""
     if dist.rank != 0:
         return None
     threads = os.cpu_count() or 1
-    n = 262144 if args.steps <= 200 else 65536
-    rate, done, el, side = cpu_oracle_rate(n, args.steps, threads, warmup=args.warmup)
-    sample = (f"c3 network at the c3 density: {n} particles in a {side:.1f} um cube, {done} steps "
-              f"({el:.1f} s) after {max(args.warmup, 1)} warm-up, OpenMP {threads} threads")
+    n = args.n or 16_000_000
+    warmup = max(args.warmup, 1)
+    rate, done, el, side = cpu_oracle_rate(n, args.steps, threads, warmup=warmup)
+    sample = (f"the full workload: c3, {n} particles in a {side:.1f} um cube, {done} steps ({el:.1f} s) after "
+              f"{warmup} warm-up, OpenMP {threads} threads; inputs derived by oracle.params (no GPU library)")
     return {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": done, "warmup": max(args.warmup, 1), "ms_per_step": el / max(done, 1) * 1e3,
+        "steps": done, "warmup": warmup, "ms_per_step": el / max(done, 1) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Philox uniform positions)",
         "config": {"workload": workload_desc("c3", args.n), "parallelism": f"cpu, {threads} threads",
-                   "sampled": "each step is a bounded sample of the workload (cpu_baseline.sample)"},
+                   "particles": n},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -347,8 +359,8 @@ def run_gb300(args, dist):
         achieved = alg / (prof[dom] / prof_steps / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind,
-                "algorithmic_bytes_per_launch": alg,
-                "traffic": traffic_from_profiles(dom, args.workload)}
+                "algorithmic_bytes_per_launch": alg}
+        roof["traffic"], roof["traffic_source"] = traffic_from_profiles(dom, args.workload)
     step_alg = sum(v for v in (algorithmic_bytes(k, n_now, n_now, n_cells, binned) for k in prof) if v)
     step_roof = {"bytes_per_step": step_alg, "achieved_gbs": step_alg / (ms / args.steps / 1e3) / 1e9,
                  "frac": step_alg / (ms / args.steps / 1e3) / 1e9 / peak}
@@ -414,14 +426,15 @@ def run_gb300(args, dist):
     # ---------------- CPU baseline (rank 0, N = 1 only)
     if not args.no_cpu and dist.rank == 0 and dist.world == 1:
         threads = os.cpu_count() or 1
-        rate, done, el, side = cpu_oracle_rate(262144, 200, threads, budget_s=20.0)
+        n = args.n or 16_000_000
+        rate, done, el, side = cpu_oracle_rate(n, 30, threads, budget_s=12.0)
         out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                               "sample": f"c3 network at the c3 density: 262144 particles in a {side:.1f} um cube,"
-                                         f" {done} steps ({el:.1f} s), OpenMP {threads} threads"}
-        # the same sample on one core
-        rate1, done1, el1, _ = cpu_oracle_rate(262144, 200, 1, budget_s=10.0)
+                               "sample": f"the c3 workload itself ({n} particles in a {side:.1f} um cube), {done} "
+                                         f"steps ({el:.1f} s) after 1 warm-up, OpenMP {threads} threads"}
+        # one step of the same workload on one core
+        rate1, done1, el1, _ = cpu_oracle_rate(n, 1, 1, warmup=0)
         out["cpu_baseline"]["single_core"] = {"value": rate1, "unit": UNIT, "cores": 1,
-                                              "sample": f"the same sample, {done1} steps ({el1:.1f} s), 1 thread"}
+                                              "sample": f"the same workload, {done1} step ({el1:.1f} s), 1 thread"}
     return out
 
 

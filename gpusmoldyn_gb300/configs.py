@@ -167,17 +167,24 @@ def c3_species(n, frac):
     return np.repeat(np.arange(len(frac), dtype=np.int32), cnt)
 
 
+def c3_reactions(density, network_seed=3):
+    """Diffusion coefficients, the 12 reactions (order, reactants, products,
+    rate) in the order they are added -- the two zeroth-order productions
+    first -- and the stationary species fractions of the c3 network at
+    `density`."""
+    D, rx = c3_network(network_seed)
+    z, frac = c3_steady_state(rx, density)
+    return D, [(0, [], [0], z), (0, [], [1], z)] + [(o, rc, pr, float(k)) for o, rc, pr, k in rx], frac
+
+
 def c3_add_network(s, density, network_seed=3):
     """Species and the 12 reactions of the c3 network on a System; returns
     the stationary species fractions."""
-    D, rx = c3_network(network_seed)
+    D, rx, frac = c3_reactions(density, network_seed)
     for d in D:
         s.add_species(float(d))
-    z, frac = c3_steady_state(rx, density)
-    s.add_reaction(0, [], [0], z)
-    s.add_reaction(0, [], [1], z)
     for order, rc, pr, k in rx:
-        s.add_reaction(order, rc, pr, float(k))
+        s.add_reaction(order, rc, pr, k)
     return frac
 
 

@@ -349,13 +349,21 @@ BD_API bd_status bd_instance_state(bd_handle h, int slot, uint32_t *steps, uint3
  * inside a cell.  d_out receives the n sorted records and d_cell_start the
  * n_cells + 1 cell starts; both are the caller's device buffers, and the
  * call is enqueued on `stream` (a cudaStream_t; NULL = legacy default).
- * Nothing is allocated: the per-cell counts and scan partials live in one
- * file-scope device array of 2^20 + 256 words (about 4 MiB) that every GPU
- * loading the library keeps until the process exits.  More than 2^20 cells
- * returns BD_ERR_CAPACITY.  The first call on a device looks up that array's
- * device address (cudaGetSymbolAddress), so make the first call before any
- * stream capture.  Calls share the array and each clears its counts first;
- * calls that overlap on the GPU race on it and must be serialised. */
+ * Nothing is allocated: the per-cell counts, scan partials and two control
+ * words live in one file-scope device array of 2^20 + 258 words (about
+ * 4 MiB) that every GPU loading the library keeps until the process exits.
+ * More than 2^20 cells (or any single dims[a] above 2^20) or more than
+ * 2^31 - 1 records returns BD_ERR_CAPACITY before anything is enqueued.
+ * d_in, d_out and d_cell_start must be disjoint (an overlap returns
+ * BD_ERR_INVALID_ARGUMENT): the kernels read the input while they write the
+ * outputs.  Ordering inside a cell is bounded work: a cell of up to 32
+ * records costs one thread at most 496 comparisons, a larger cell is sorted
+ * by one thread block with a bitonic network, O(m log^2 m) for m records.
+ * The first call on a device (and the first after a device reset, which
+ * reloads the module) looks up that array's device address
+ * (cudaGetSymbolAddress), so make the first call before any stream capture.
+ * Calls share the array and each clears its counts first; calls that
+ * overlap on the GPU race on it and must be serialised. */
 BD_API bd_status bd_cell_sort_static(const float *d_in, uint64_t n, const float box_lo[3], const float box_hi[3],
                                      const uint32_t dims[3], float *d_out, uint32_t *d_cell_start, void *stream);
 

@@ -5,7 +5,9 @@
   operation is a single IEEE operation, with OpenMP when available.
 * ``build_ref(ref_dir)`` compiles ref_kat.cpp against the reference's own
   host sources *where they lie* in ``ref_dir`` (nothing is copied) into
-  ``oracle/_ref/ref_kat``.  It is skipped when the reference tree is absent.
+  ``oracle/_ref/ref_kat``.  ``ref_dir`` defaults to $REF_DIR, else to a
+  ``reference`` directory beside the repository.  It is skipped when the
+  reference tree is absent.
 """
 from __future__ import annotations
 
@@ -45,7 +47,7 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_ref(ref_dir: str | None = None, force: bool = False) -> str | None:
-    ref_dir = ref_dir or os.environ.get("REF_DIR", "/root/reference")
+    ref_dir = ref_dir or os.environ.get("REF_DIR") or os.path.join(HERE, "..", "..", "reference")
     if not os.path.exists(os.path.join(ref_dir, "rxnparam.cpp")):
         return None
     if not force and os.path.exists(REF_KAT) and os.path.getmtime(REF_KAT) >= os.path.getmtime(

@@ -1,9 +1,11 @@
 """ctypes wrapper of liboracle.so -- TEST INFRASTRUCTURE, not product.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
-this module.  ``system_from(sys)`` reads a configured library handle's
+this module.  ``OracleSystem(sys)`` reads a configured library handle's
 parameters through the public C ABI (species D, reaction table entries,
-grid, Poisson CDFs, normal table) and turns them into the oracle's inputs.
+grid, Poisson CDFs, normal table) and turns them into the oracle's inputs;
+``OracleSystem.from_network`` derives them instead with ``oracle.params``
+from a network description alone, without loading the library.
 """
 from __future__ import annotations
 
@@ -93,30 +95,11 @@ class OracleSystem:
             pos += len(cdf)
         cdf_all = np.concatenate(cdfs) if pos else np.zeros(1)
         gauss = gauss_table()
-        arrs = dict(order=order, react0=react0, react1=react1, prod0=prod0, prod1=prod1, prob=prob,
-                    bind_radius=brad, off0=off0, off1=off1, thresh=thresh, D=D.astype(np.float32), gauss=gauss,
-                    cdf=cdf_all.astype(np.float64), cdf_off=np.array(coff or [0], np.int32),
-                    cdf_len=np.array(clen or [0], np.int32), cdf_kmin=np.array(ckmin or [0], np.int32))
-        self.arrs = arrs
-        s = or_system()
-        for a in range(3):
-            s.lo[a] = d["box_lo"][a]
-            s.hi[a] = d["box_hi"][a]
-            s.inv[a] = inv[a]
-            s.cell[a] = cell[a]
-            s.dims[a] = int(dims[a])
-        seed = int(d.get("seed", 1))
-        s.key_lo = seed & 0xFFFFFFFF
-        s.key_hi = seed >> 32
-        s.normal_mode = sys.cfg.normal_mode
-        s.S = sys.n_species
-        s.dt = sys.dt
-        s.R = R
-        for name in ("order", "react0", "react1", "prod0", "prod1", "cdf_off", "cdf_len", "cdf_kmin"):
-            setattr(s, name, arrs[name].ctypes.data_as(ip))
-        for name in ("prob", "bind_radius", "off0", "off1", "thresh", "D", "gauss"):
-            setattr(s, name, arrs[name].ctypes.data_as(fp))
-        s.cdf = arrs["cdf"].ctypes.data_as(dp)
+        self._fill(order, react0, react1, prod0, prod1, prob, brad, off0, off1, thresh, D, gauss, cdf_all, coff,
+                   clen, ckmin)
+        arrs = self.arrs
+        s = self._system(d["box_lo"], d["box_hi"], dims, cell, inv, int(d.get("seed", 1)), sys.cfg.normal_mode,
+                         sys.n_species, sys.dt, R)
         # surfaces: the panels' derived geometry (bd_panel_info words) and the
         # [surface][species][front, back] action table, read through the C ABI
         n_surf, n_pan = sys.surface_counts()
@@ -145,6 +128,84 @@ class OracleSystem:
         self.s = s
         self.n_cells = int(dims[0]) * int(dims[1]) * int(dims[2])
         self.R = R
+
+    def _fill(self, order, react0, react1, prod0, prod1, prob, brad, off0, off1, thresh, D, gauss, cdf_all, coff,
+              clen, ckmin):
+        self.keep = []
+        self.arrs = dict(order=order, react0=react0, react1=react1, prod0=prod0, prod1=prod1, prob=prob,
+                         bind_radius=brad, off0=off0, off1=off1, thresh=thresh, D=np.asarray(D, np.float32),
+                         gauss=gauss, cdf=np.asarray(cdf_all, np.float64), cdf_off=np.array(coff or [0], np.int32),
+                         cdf_len=np.array(clen or [0], np.int32), cdf_kmin=np.array(ckmin or [0], np.int32))
+
+    def _system(self, lo, hi, dims, cell, inv, seed, normal_mode, S, dt, R):
+        arrs = self.arrs
+        s = or_system()
+        for a in range(3):
+            s.lo[a] = lo[a]
+            s.hi[a] = hi[a]
+            s.inv[a] = inv[a]
+            s.cell[a] = cell[a]
+            s.dims[a] = int(dims[a])
+        s.key_lo = seed & 0xFFFFFFFF
+        s.key_hi = seed >> 32
+        s.normal_mode = normal_mode
+        s.S = S
+        s.dt = dt
+        s.R = R
+        for name in ("order", "react0", "react1", "prod0", "prod1", "cdf_off", "cdf_len", "cdf_kmin"):
+            setattr(s, name, arrs[name].ctypes.data_as(ip))
+        for name in ("prob", "bind_radius", "off0", "off1", "thresh", "D", "gauss"):
+            setattr(s, name, arrs[name].ctypes.data_as(fp))
+        s.cdf = arrs["cdf"].ctypes.data_as(dp)
+        return s
+
+    @classmethod
+    def from_network(cls, D, reactions, box_lo, box_hi, dt, seed, n_particles, normal_mode=0, threads=0,
+                     d_scale=1.0, k2_scale=1.0, occupancy=3.0, cell_size=0.0):
+        """An oracle whose inputs are derived by oracle.params from a network
+        description: D per species and a list of oracle.params.Reaction.  The
+        grid is planned for n_particles; no library is loaded."""
+        from . import params as P
+
+        self = cls.__new__(cls)
+        R = len(reactions)
+        vol = np.float32(np.float32(box_hi[0] - box_lo[0]) * np.float32(box_hi[1] - box_lo[1])) \
+            * np.float32(box_hi[2] - box_lo[2])
+        der = P.derive(D, reactions, dt, vol, d_scale, k2_scale)
+        if der["status"]:
+            raise RuntimeError(f"oracle.params: set-up error {der['status']}")
+        r_max = max([float(der["bind_radius"][r]) for r in range(R) if reactions[r].order == 2] or [0.0])
+        dims, cell, inv = P.plan_grid(box_lo, box_hi, n_particles, r_max, occupancy, cell_size)
+        col = lambda f, dt_: np.array([f(q) for q in reactions] or [0], dt_)  # noqa: E731
+        cdfs, coff, clen, ckmin, pos = [], [], [], [], 0
+        for r in range(R):
+            c = der["cdf"][r] if reactions[r].order == 0 else np.zeros(0)
+            cdfs.append(c)
+            coff.append(pos)
+            clen.append(len(c))
+            ckmin.append(der["cdf_kmin"][r] if reactions[r].order == 0 else 0)
+            pos += len(c)
+        gauss = P.gauss_quantiles() if normal_mode == 1 else np.zeros(4096, np.float32)
+        self._fill(col(lambda q: q.order, np.int32), col(lambda q: q.reactants[0], np.int32),
+                   col(lambda q: q.reactants[1], np.int32), col(lambda q: q.products[0], np.int32),
+                   col(lambda q: q.products[1], np.int32), der["prob"] if R else np.zeros(1, np.float32),
+                   der["bind_radius"] if R else np.zeros(1, np.float32), der["off0"] if R else np.zeros(1, np.float32),
+                   der["off1"] if R else np.zeros(1, np.float32), np.ones(max(R, 1), np.float32), der["D"], gauss,
+                   np.concatenate(cdfs) if pos else np.zeros(1), coff, clen, ckmin)
+        s = self._system(box_lo, box_hi, dims, cell, inv, int(seed), normal_mode, len(D), dt, R)
+        s.n_panels = 0
+        s.panels = None
+        s.surf_act = None
+        s.sorted = 1 if any(q.order in (1, 2) or (q.order == 0 and q.nprod == 2) for q in reactions) else 0
+        s.inst = 0
+        s.threads = threads
+        s.channels = 0
+        self.s = s
+        self.n_cells = int(dims[0]) * int(dims[1]) * int(dims[2])
+        self.R = R
+        self.grid = (dims, cell, inv)
+        self.derived = der
+        return self
 
     def step(self, t, recs, want_cells=False, want_pairs=False, cap=None, events=None):
         """Advance records (n x 4 uint32: x, y, z bits and w) by one step."""

@@ -2,8 +2,9 @@
 
 Builds oracle/_ref/ref_kat from the reference's host sources (rxnparam,
 smolreact, stats, SFMT, dcmt, reaction_cpu) where they lie and stores its
-output.  Needs the reference tree (REF_DIR, default /root/reference); the
-committed JSON lets every other machine run the pins without it.
+output.  Needs the reference tree ($REF_DIR, else a ``reference`` directory
+beside the repository); the committed JSON lets every other machine run the
+pins without it.
 """
 import json
 import os

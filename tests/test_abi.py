@@ -91,3 +91,28 @@ def test_invalid_arguments():
     s.finalize()
     with pytest.raises(L.BDError):
         s.set_particles(np.full((1, 3), 2.0, np.float32), np.zeros(1, np.int32))  # outside the box
+
+
+def _static_sort_args(dims, d_in, d_out, d_start, n=4):
+    lo = (C.c_float * 3)(0.0, 0.0, 0.0)
+    hi = (C.c_float * 3)(1.0, 1.0, 1.0)
+    dm = (C.c_uint32 * 3)(*dims)
+    return (C.c_void_p(d_in), n, lo, hi, dm, C.c_void_p(d_out), C.c_void_p(d_start), None)
+
+
+def test_static_sort_rejects_wrapping_and_overlapping_arguments():
+    """The allocation-free sort checks its grid and buffers before it touches
+    the GPU: these calls return before any CUDA call, with placeholder
+    addresses that are never dereferenced."""
+    lib = L.load()
+    a, b, c = 1 << 20, 2 << 20, 3 << 20
+    # 2^22 * 2^22 * 2^20 = 2^64 wraps a 64-bit product to 0
+    assert lib.bd_cell_sort_static(*_static_sort_args((1 << 22, 1 << 22, 1 << 20), a, b, c)) == L.BD_ERR_CAPACITY
+    assert lib.bd_cell_sort_static(*_static_sort_args((1 << 21, 1, 1), a, b, c)) == L.BD_ERR_CAPACITY
+    assert lib.bd_cell_sort_static(*_static_sort_args((128, 128, 65), a, b, c)) == L.BD_ERR_CAPACITY
+    assert lib.bd_cell_sort_static(*_static_sort_args((0, 4, 4), a, b, c)) == L.BD_ERR_INVALID_ARGUMENT
+    # in place, and cell starts inside the record buffers
+    assert lib.bd_cell_sort_static(*_static_sort_args((4, 4, 4), a, a, c)) == L.BD_ERR_INVALID_ARGUMENT
+    assert lib.bd_cell_sort_static(*_static_sort_args((4, 4, 4), a, a + 32, c)) == L.BD_ERR_INVALID_ARGUMENT
+    assert lib.bd_cell_sort_static(*_static_sort_args((4, 4, 4), a, b, b + 16)) == L.BD_ERR_INVALID_ARGUMENT
+    assert lib.bd_cell_sort_static(*_static_sort_args((4, 4, 4), a, b, a + 60)) == L.BD_ERR_INVALID_ARGUMENT

@@ -95,3 +95,31 @@ def test_static_sort_rejects_grids_beyond_its_scratch():
     rc = lib.bd_cell_sort_static(C.c_void_p(buf.data_ptr()), 4, lo, hi, dm, C.c_void_p(buf.data_ptr()),
                                  C.c_void_p(start.data_ptr()), None)
     assert rc == L.BD_ERR_CAPACITY
+
+
+def crowded_dataset(seed, n):
+    """Uniform records plus two crowded cells: about 2,000 records in one
+    (ordered in shared memory) and 5,000 in another (ordered in place in
+    global memory), some of them exact duplicates."""
+    pos, species = dataset(seed, n)
+    g = rng(seed + 100)
+    a = (1.1 + 0.3 * g.random((2000, 3))).astype(np.float32)      # inside cell [1.0, 1.5)^3
+    b = (6.05 + 0.4 * g.random((5000, 3))).astype(np.float32)     # inside cell [6.0, 6.5)^3
+    b[:700] = b[700:1400]
+    pos = np.concatenate([pos, a, b])
+    species = np.concatenate([species, np.arange(7000, dtype=np.int32) % 3])
+    perm = g.permutation(len(pos))
+    return pos[perm], species[perm]
+
+
+def test_static_sort_orders_crowded_cells():
+    cell = 0.5
+    for call, (seed, n) in enumerate(((41, 30000), (42, 12345))):
+        pos, sp = crowded_dataset(seed, n)
+        xyz, w, cells, dims = handle_sort(pos, sp, cell)
+        out, start = static_sort(pos, sp, dims)
+        assert np.max(np.diff(start.astype(np.int64))) >= 5000
+        np.testing.assert_array_equal(start, cells, err_msg=f"call {call}: cell starts")
+        np.testing.assert_array_equal(out[:, :3].view(np.uint32), xyz.view(np.uint32),
+                                      err_msg=f"call {call}: positions")
+        np.testing.assert_array_equal(out[:, 3].view(np.uint32), w, err_msg=f"call {call}: species words")
