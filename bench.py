@@ -57,7 +57,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--no-surfaces", action="store_true")
-    p.add_argument("--serve-jobs", type=int, default=40)
+    p.add_argument("--serve-jobs", type=int, default=200)
     p.add_argument("--profile-only", action="store_true", help="build + a few steps (for ncu)")
     p.add_argument("--profile-surfaces", action="store_true",
                    help="with --profile-only: the c3 step inside the cell (k_bin_surface)")
@@ -382,13 +382,16 @@ def run_gb300(args, dist):
     # ---------------- end to end through the C ABI with host buffers
     if not args.no_e2e:
         s3, pos, sp = network_and_particles(args.workload, args.n, device)
-        # the caller's arrays in the reference's layout: float4 positions, int species
-        pos4 = np.zeros((len(sp), 4), np.float32)
+        # the caller's arrays in the reference's layout (float4 positions, int
+        # species) in pinned host memory, and the arrays it reads the result
+        # into, kept across calls (as the reference's m_hPos / m_hTypes)
+        pos4 = pinned((len(sp), 4), np.float32)
         pos4[:, :3] = pos
-        sp = np.ascontiguousarray(sp, np.int32)
-        # and the arrays it reads the result into, kept across calls (as the
-        # reference's m_hPos / m_hTypes)
-        out4 = (np.full((2 * len(sp), 4), -1.0, np.float32), np.full(2 * len(sp), -1, np.int32))
+        pos4[:, 3] = 0.0
+        sp4 = pinned((len(sp),), np.int32)
+        sp4[:] = sp
+        sp = sp4
+        out4 = (pinned((2 * len(sp), 4), np.float32), pinned((2 * len(sp),), np.int32))
         dist.barrier()
         t0 = time.perf_counter()
         s3.set_particles(pos4, sp)
@@ -407,7 +410,7 @@ def run_gb300(args, dist):
         out["e2e"] = {"value": dist.sum(psteps) / e2e_s, "unit": UNIT,
                       "h2d_bytes_per_step": 20 * len(sp) / args.steps,
                       "d2h_bytes_per_step": 8 + 20 * len(sp_out) / args.steps,
-                      "path": "bd_set_particles + steps x (bd_step(1) + bd_get_count) + bd_get_particles",
+                      "path": "bd_set_particles + steps x (bd_step(1) + bd_get_count) + bd_get_particles, pinned host arrays",
                       "seconds": {"set_particles": ta - t0, "steps": tb - ta, "get_particles": t1 - tb}}
         s3.close()
 
@@ -438,6 +441,16 @@ def run_gb300(args, dist):
     return out
 
 
+def pinned(shape, dtype):
+    """A numpy array over page-locked host memory (host<->device copies from
+    and into it run at the link's DMA rate instead of being staged)."""
+    import numpy as np
+    import torch
+
+    tdt = {np.float32: torch.float32, np.int32: torch.int32}[dtype]
+    return torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
+
+
 def run_surfaces(args, dist, device, plain_value):
     """The c3 step inside a cell: a spherical membrane (one sphere panel) and
     a nucleus of 1280 triangles, walked by every diffusion step."""
@@ -463,48 +476,84 @@ def run_surfaces(args, dist, device, plain_value):
 
 
 def run_batched(args, dist, device):
+    """c4: 256 instances of the c2 network as one pipeline per step.  Under
+    torchrun the instances are split across ranks by particle count
+    (sharding.my_instances, no communication); each rank tunes the cell
+    occupancy and launch shape on a scaled copy of its share (every 8th
+    instance), then runs the c4-specified 2,000 steps.  The same instances
+    are also stepped one after another as plain systems."""
     import numpy as np
 
-    from gpusmoldyn_gb300 import configs
+    from gpusmoldyn_gb300 import configs, sharding, tune
+    from gpusmoldyn_gb300.system import System
 
-    steps = max(args.steps // 4, 20)
-    s, inst, counts = configs.build_c4(device=device)
+    inst_all, counts_all = configs.c4_instances()
+    pos_all, sp_all = configs.c4_positions(inst_all, counts_all)
+    offs = np.concatenate([[0], np.cumsum(counts_all)])
+    mine = sharding.my_instances(counts_all, dist.world, dist.rank)
+
+    def share(ids):
+        inst = [inst_all[k] for k in ids]
+        counts = np.array([counts_all[k] for k in ids], np.int64)
+        pos = np.concatenate([pos_all[offs[k]:offs[k + 1]] for k in ids])
+        sp = np.concatenate([sp_all[offs[k]:offs[k + 1]] for k in ids])
+        return inst, counts, pos, sp
+
+    def build(ids, occupancy=0.0):
+        inst, counts, pos, sp = share(ids)
+        s = System(dt=5e-4, seed=4, instances=inst, cell_occupancy=occupancy, device=device)
+        configs.c2_network(s)
+        s.finalize()
+        s.set_ensemble_particles(pos, sp, counts)
+        return s
+
+    tuned = tune.tune(lambda occ: build(mine[::8], occ), steps=20, warmup=5)
+    steps = max(args.steps, 2000)
+    s = build(mine, tuned["occupancy"])
+    s.set_launch_shape(*tuned["shape"])
     s.step(args.warmup)
     s.synchronize()
     n0 = int(np.sum(s.instance_counts()))
+    dist.barrier()
     ms = s.time_steps(steps)
+    dist.barrier()
     n1 = int(np.sum(s.instance_counts()))
-    batched = steps * 0.5 * (n0 + n1) / (ms / 1e3)
+    prof = s.profile_steps(20)
+    kms = {k: v / 20 for k, v in prof.items()}
+    ms_max = dist.max(ms)
+    batched = dist.sum(steps * 0.5 * (n0 + n1)) / (ms_max / 1e3)
     s.close()
     # the same instances advanced one after another as plain systems
     loop_steps = 10
     total_ms = 0.0
     total_ps = 0.0
-    pos, sp = configs.c4_positions(inst, counts)
-    off = 0
-    for d, n in zip(inst, counts):
-        p = configs.build_c2_instance(d, n, device=device)
-        p.set_particles(pos[off:off + n], sp[off:off + n])
-        off += n
+    for k in mine:
+        inst, counts, pos, sp = share([k])
+        p = configs.build_c2_instance(inst[0], int(counts[0]), device=device)
+        p.set_particles(pos, sp)
         p.step(3)
         p.synchronize()
         total_ms += p.time_steps(loop_steps)
-        total_ps += loop_steps * int(n)
+        total_ps += loop_steps * int(counts[0])
         p.close()
-    loop = total_ps / (total_ms / 1e3)
-    return {"workload": f"c4: {len(inst)} instances of the c2 network, {int(np.sum(counts))} particles",
-            "value": batched, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
+    loop = dist.sum(total_ps) / (dist.max(total_ms) / 1e3)
+    return {"workload": f"c4: {len(inst_all)} instances of the c2 network, {int(np.sum(counts_all))} particles"
+                        + (f", split over {dist.world} ranks by particle count" if dist.world > 1 else ""),
+            "value": batched, "unit": UNIT, "steps": steps, "ms_per_step": ms_max / steps,
+            "kernel_ms_per_step": kms, "launch_gaps_ms_per_step": ms / steps - sum(kms.values()),
+            "tuned": {"cell_occupancy": tuned["occupancy"], "launch_shape": list(tuned["shape"]),
+                      "tuning_s": round(tuned["tuning_s"], 2), "tuned_on": f"every 8th instance of the share "
+                                                                           f"({len(mine[::8])} instances)"},
             "plain_loop_value": loop, "speedup_vs_plain_loop": batched / loop}
 
 
 def run_serving(args, device):
     """c5: Poisson arrivals at 50/s of c3-network simulations with N
     log-uniform in 1e3-5e6 and steps uniform in 100-10000, admitted into one
-    serving handle against a 150 GB budget."""
+    serving handle against a 150 GB budget; then the same requests served
+    one at a time as plain systems (the baseline)."""
     from gpusmoldyn_gb300 import configs
-    from gpusmoldyn_gb300.serve import Server
-
-    from gpusmoldyn_gb300.serve import c3_request
+    from gpusmoldyn_gb300.serve import Server, c3_request, run_sequential
 
     jobs = configs.c5_jobs(args.serve_jobs, seed=5)
     # each request arrives with its initial state (the client builds it)
@@ -513,10 +562,15 @@ def run_serving(args, device):
     srv = Server(max_instances=64, hbm_budget=150e9, chunk=10, device=device)
     res = srv.run(jobs)
     srv.close()
+    seq = run_sequential(jobs, device=device)
     return {"workload": f"c5: {len(jobs)} requests, Poisson 50/s, N log-U[1e3, 5e6], steps U[100, 10000]",
             "p50_latency_s": res["p50_s"], "p99_latency_s": res["p99_s"], "mean_latency_s": res["mean_s"],
             "value": res["particle_steps_per_s"], "unit": UNIT, "wall_s": res["wall_s"], "jobs": res["jobs"],
-            "seconds": {k: round(v, 4) for k, v in res["host_seconds"].items()}}
+            "seconds": {k: round(v, 4) for k, v in res["host_seconds"].items()},
+            "one_at_a_time": {"p50_latency_s": seq["p50_s"], "p99_latency_s": seq["p99_s"],
+                              "mean_latency_s": seq["mean_s"], "value": seq["particle_steps_per_s"],
+                              "wall_s": seq["wall_s"]},
+            "speedup_vs_one_at_a_time": res["particle_steps_per_s"] / seq["particle_steps_per_s"]}
 
 
 def main():

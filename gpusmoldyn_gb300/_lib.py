@@ -127,6 +127,7 @@ _SIGS = {
     "bd_instance_cancel": (C.c_int, [H, C.c_int]),
     "bd_get_instance_counts": (C.c_int, [H, P, C.c_int]),
     "bd_get_species_counts": (C.c_int, [H, C.c_int, P, C.c_int]),
+    "bd_measure_msd": (C.c_int, [H, C.c_int, C.c_int, P, P, C.c_int]),
     "bd_get_state_pointer": (C.c_int, [H, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)]),
     "bd_step": (C.c_int, [H, C.c_int]),
     "bd_step_async": (C.c_int, [H, C.c_int, P]),

@@ -126,7 +126,9 @@ struct bd_system {
   DevBuf<uint32_t> inst_step, inst_slot_base, zero_off;
   DevBuf<unsigned long long> events, pending;
   DevBuf<float4> state0, state1, scatter, bins;
-  DevBuf<uint32_t> best, cell_count, cell_start, tile_sums, big;
+  DevBuf<unsigned long long> best;
+  DevBuf<uint32_t> cell_count, cell_start, tile_sums, big;
+  DevBuf<uint4> match_list;
   DevBuf<unsigned long long> scan_flags;
   DevBuf<float4> big_scratch;  // allocated when a cell first outgrows the pair kernel
   DevBuf<DevPair> pairs;
@@ -205,6 +207,7 @@ KParams make_params(bd_system* h) {
   p.scan_withhold = h->scan_withhold ? 1u : 0u;
   p.pairs = h->pairs.p;
   p.best = h->best.p;
+  p.match_list = h->match_list.p;
   p.events = h->events.p;
   p.pending = h->pending.p;
   p.n_inst = (uint32_t)h->n_inst();
@@ -392,12 +395,12 @@ bd_status push_ctrl(bd_system* h) {
 bd_status grow_particles(bd_system* h, uint64_t cap) {
   if (cap > 0xFFFFFFF0ull) return BD_ERR_CAPACITY;
   DevBuf<float4> s0, s1, sc;
-  DevBuf<uint32_t> best;
+  DevBuf<unsigned long long> best;
   BD_CUDA(s0.alloc(cap));
   BD_CUDA(s1.alloc(cap));
   if (!h->binned) BD_CUDA(sc.alloc(cap));
   BD_CUDA(best.alloc(cap));
-  BD_CUDA(cudaMemsetAsync(best.p, 0xFF, cap * sizeof(uint32_t), h->stream));
+  BD_CUDA(cudaMemsetAsync(best.p, 0xFF, cap * sizeof(unsigned long long), h->stream));
   if (!h->panels.empty()) BD_CUDA(h->surf_queue.alloc(cap));
   // cells above 128 records (the large-cell kernel's queue) number at most cap / 129
   BD_CUDA(h->big.alloc(cap / 129 + 2));
@@ -425,6 +428,7 @@ bd_status grow_particles(bd_system* h, uint64_t cap) {
 
 bd_status grow_pairs(bd_system* h, uint32_t cap) {
   BD_CUDA(h->pairs.alloc(cap));
+  BD_CUDA(h->match_list.alloc(2 * (uint64_t)cap));
   h->pair_cap = cap;
   return BD_OK;
 }
@@ -713,6 +717,7 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->tile_sums.free();
   h->scan_flags.free();
   h->pairs.free();
+  h->match_list.free();
   h->dpanels.free();
   h->dsurf_act.free();
   h->dpbox_start.free();
@@ -1154,6 +1159,70 @@ BD_API bd_status bd_step(bd_handle h, int nsteps) {
   }
   while (left-- > 0) BD_CUDA(cudaGraphLaunch(h->graph1, h->stream));
   h->target_step += (uint64_t)nsteps;
+  return BD_OK;
+}
+
+BD_API bd_status bd_measure_msd(bd_handle h, int inst, int nsteps, double* msd, uint64_t* counts, int n) {
+  const Range range("bd_measure_msd");
+  if (!h || nsteps < 0 || n < 0 || inst < -1) return BD_ERR_INVALID_ARGUMENT;
+  if (!h->finalized) return BD_ERR_NOT_FINALIZED;
+  if (inst >= h->n_inst()) return BD_ERR_INVALID_ARGUMENT;
+  for (int s = 0; s < n; s++) {
+    if (msd) msd[s] = 0.0;
+    if (counts) counts[s] = 0;
+  }
+  if (h->host_only) return BD_ERR_NO_DEVICE;
+  if (!h->have_particles) return BD_ERR_NOT_FINALIZED;
+  if (!h->panels.empty()) return BD_ERR_UNSUPPORTED;  // the move would also need the surface walk
+  BD_CUDA(cudaSetDevice(h->device));
+  bd_status st = bd_synchronize(h);
+  if (st && st != BD_ERR_EMPTY) return st;
+  if (!h->graph1) {
+    st = build_graphs(h);
+    if (st) return st;
+  }
+  const size_t m = (size_t)h->n_inst() * h->S;
+  DevBuf<double> sum;
+  DevBuf<unsigned long long> cnt;
+  BD_CUDA(sum.alloc(m));
+  BD_CUDA(cnt.alloc(m));
+  BD_CUDA(cudaMemsetAsync(sum.p, 0, m * sizeof(double), h->stream));
+  BD_CUDA(cudaMemsetAsync(cnt.p, 0, m * sizeof(unsigned long long), h->stream));
+  const bool table = h->cfg.normal_mode == BD_NORMALS_TABLE;
+  for (int k = 0; k < nsteps; k++) {
+    // one step at a time, synchronised: a step that overflows is replayed
+    // by bd_synchronize at once (with grown buffers, so the parameters are
+    // taken again); its moves were measured before it first ran and the
+    // replay repeats the same moves unmeasured
+    enqueue_msd(make_params(h), table, sum.p, cnt.p, h->stream);
+    BD_CUDA(cudaGetLastError());
+    if (!h->graph1) {
+      st = build_graphs(h);
+      if (st) return st;
+    }
+    BD_CUDA(cudaGraphLaunch(h->graph1, h->stream));
+    h->target_step += 1;
+    st = bd_synchronize(h);
+    if (st && st != BD_ERR_EMPTY) return st;
+  }
+  std::vector<double> hs(m);
+  std::vector<unsigned long long> hc(m);
+  BD_CUDA(cudaMemcpyAsync(hs.data(), sum.p, m * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  BD_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, m * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  BD_CUDA(cudaStreamSynchronize(h->stream));
+  sum.free();
+  cnt.free();
+  for (int s = 0; s < std::min(n, h->S); s++) {
+    double a = 0.0;
+    unsigned long long b = 0;
+    for (int k = 0; k < h->n_inst(); k++) {
+      if (inst >= 0 && k != inst) continue;
+      a += hs[(size_t)k * h->S + s];
+      b += hc[(size_t)k * h->S + s];
+    }
+    if (msd) msd[s] = b ? a / (double)b : 0.0;
+    if (counts) counts[s] = b;
+  }
   return BD_OK;
 }
 

@@ -41,8 +41,7 @@ namespace bd {
 namespace {
 
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;
-constexpr uint32_t kFree = 0xFFFFFFFFu;
-constexpr uint32_t kMatched = 0xFFFFFFFEu;
+constexpr unsigned long long kFree64 = ~0ull;  // matcher word of a record not in a pending pair
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -791,9 +790,68 @@ struct CellView {
   }
 };
 
+// A cell's bin with its first kBinGroup places staged in shared memory by
+// a bulk copy (kStage); the rest of the bin is read from global memory.
+template <bool kStage>
+struct BinView {
+  const float4* sm;
+  CellView g;
+  __device__ __forceinline__ float4 operator[](uint32_t m) const {
+    if (kStage && m < kBinGroup) return sm[m];
+    return g[m];
+  }
+  __device__ __forceinline__ float4 ldg(uint32_t m) const {
+    if (kStage && m < kBinGroup) return sm[m];
+    return g.ldg(m);
+  }
+  __device__ __forceinline__ float ldg_x(uint32_t m) const {
+    if (kStage && m < kBinGroup) return sm[m].x;
+    return g.ldg_x(m);
+  }
+};
+
+// Bulk global -> shared copies completed on an mbarrier (the copy engine
+// moves the bytes; no thread issues a load per word).
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
+  return (uint32_t)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// One thread: announce `bytes` and start the copy that will deliver them.
+// The fence orders this thread's earlier generic-proxy accesses of the
+// buffer (the warp's reads of its previous contents) before the copy.
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+// Wait for the phase with parity `parity` of `bar` to complete; false after
+// 2^20 polls (each poll suspends the thread for at most a short
+// hardware-defined time).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 20); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // Position of record r among the records of its cell [s, e) in canonical
 // order; ties between identical records go by slot.
-__device__ __forceinline__ uint32_t canonical_rank(const CellView sc, uint32_t s, uint32_t e, uint32_t slot,
+template <class View>
+__device__ __forceinline__ uint32_t canonical_rank(const View sc, uint32_t s, uint32_t e, uint32_t slot,
                                                    const float4& r) {
   uint32_t rank = 0;
   for (uint32_t m = s; m < e; ++m) {
@@ -892,6 +950,24 @@ __device__ __forceinline__ void emit(const KParams& p, DevCtrl* c, const Seeker&
                                      int32_t b) {
   emit_pair(p, c, min(ca, cq), max(ca, cq), b, __ldg(&p.bim[k.block * p.B + (uint32_t)b].prob), k.inst,
             inst_of<kSingle>(p, k.inst));
+}
+
+// True when record k may lie within its largest binding radius (plus the
+// pruning margin) of a +x, +y or +z face of its cell, i.e. when
+// forward_mask may return a neighbour; false for most records, which lie
+// deeper inside their cell.  The test runs on the fractional grid
+// coordinates: frac = g - floor(g) is exact (Sterbenz), and the 1% slack
+// exceeds the rounding of forward_mask's face distances, so it never
+// rejects a record that forward_mask would give a neighbour.
+template <bool kSingle>
+__device__ __forceinline__ bool near_forward_face(const KParams& p, const Seeker& k) {
+  const DevInstance& I = inst_of<kSingle>(p, k.inst);
+  const float gx = __fmul_rn(__fsub_rn(k.r.x, I.lo[0]), I.inv[0]);
+  const float gy = __fmul_rn(__fsub_rn(k.r.y, I.lo[1]), I.inv[1]);
+  const float gz = __fmul_rn(__fsub_rn(k.r.z, I.lo[2]), I.inv[2]);
+  const float slack = 1.01f * (k.max_r + p.prune_margin * fminf(I.cell[0], fminf(I.cell[1], I.cell[2])));
+  return !(1.0f - (gx - floorf(gx)) > slack * I.inv[0] && 1.0f - (gy - floorf(gy)) > slack * I.inv[1] &&
+           1.0f - (gz - floorf(gz)) > slack * I.inv[2]);
 }
 
 // The forward neighbour cells (higher key) of record k that its largest
@@ -999,47 +1075,78 @@ __device__ __forceinline__ void visit_neighbour(const KParams& p, DevCtrl* c, co
 //   * in the same loop marks the cell's later records (storage order)
 //     whose x lies within its largest binding radius; only those are read
 //     in full and tested, each in-cell pair once;
-//   * marks the forward neighbour cells its binding radius reaches
-//     (forward_mask) and queues one visit per cell in the warp's shared
-//     queue; the warp visits them 32 at a time, one per lane, so the few
-//     records near a face do not hold the whole warp through a visit's
-//     chain of dependent loads (cell start, records, tables).
+//   * tests, cheaply and with no branch, whether its record lies within
+//     its largest binding radius of a +face of its cell (near_forward_face)
+//     and queues those few records in the warp's shared queue; the warp
+//     takes them 32 at a time, one per lane, marks their forward neighbour
+//     cells (forward_mask) and visits them.  Marking the neighbours of
+//     every record in line, and visiting them from the record's own lane,
+//     held whole warps for the sake of one or two lanes.
 // Canonical slots of partners are computed only for pairs within range.
 // Cells above kBigCell records are queued for the large-cell kernels.  kBinned: the
 // records come from the cell bins, whose counts are cleared here for the
 // next step; otherwise from the compact scatter buffer.
-constexpr uint32_t kVisitQueue = 64;  // queued visits per warp (< 32 between drains, + one round's push)
+//
+// Binned path: bulk-copy staging of each task's first bin group (kStage).
+// Measured slower on the 16M c3 step (0.360 against 0.338 ms): four CTAs'
+// staging buffers take the L1 space that the neighbour visits hit in.  Kept
+// selectable.
+constexpr bool kStagePairs = false;
 
-// Visits queued by a warp: the visit of queue entry `lane`.
-struct VisitQueue {
-  float4 rec[kVisitQueue];
-  uint32_t ca[kVisitQueue], key[kVisitQueue];
+constexpr uint32_t kFaceQueue = 64;  // queued records per warp (< 32 between drains, + one round's push)
+
+// Records near a +face queued by a warp.
+struct FaceQueue {
+  float4 rec[kFaceQueue];
+  uint32_t ca[kFaceQueue];
 };
 
-// Visit the first 32 queued entries, one per lane, and move the rest
-// (vq - 32 < 32 entries) to the front.  Warp-uniform call.
+// Take the first 32 queued records, one per lane (lane < n), move the rest
+// (n - 32 < 32 entries) to the front, then mark and visit the forward
+// neighbour cells of the lane's record.  Warp-uniform call.
 template <bool kBinned, bool kSingle>
-__device__ __forceinline__ void drain_visits(const KParams& p, DevCtrl* c, VisitQueue& q, uint32_t vq,
-                                             const float* s_maxr, bool adv0) {
+__device__ __forceinline__ void drain_faces(const KParams& p, DevCtrl* c, FaceQueue& q, uint32_t n,
+                                            const float* s_maxr, bool adv0) {
   const uint32_t lane = lane_id();
   __syncwarp();
   const float4 r = q.rec[lane];
-  const uint32_t ca = q.ca[lane], key = q.key[lane];
+  const uint32_t ca = q.ca[lane];
   __syncwarp();
-  if (lane + 32u < vq) {
+  if (lane + 32u < n) {
     q.rec[lane] = q.rec[lane + 32u];
     q.ca[lane] = q.ca[lane + 32u];
-    q.key[lane] = q.key[lane + 32u];
   }
   __syncwarp();
-  visit_neighbour<kBinned, kSingle>(p, c, r, ca, key, s_maxr, adv0);
+  if (lane >= n) return;
+  Seeker k;
+  if (!seeker_init<kSingle>(p, r, k, s_maxr, adv0)) return;
+  uint32_t key0 = 0;
+  uint32_t nbm = forward_mask<kSingle>(p, k, &key0);
+  const DevInstance& I = inst_of<kSingle>(p, k.inst);
+  while (nbm) {
+    const uint32_t nkey = forward_key(key0, (uint32_t)(__ffs(nbm) - 1), I.dims[0], I.dims[1]);
+    nbm &= nbm - 1u;
+    visit_neighbour<kBinned, kSingle>(p, c, r, ca, nkey, s_maxr, adv0);
+  }
 }
 
-template <bool kHasBim, bool kBinned, bool kSingle>
+// kStage (binned path): group 0 of a task's 32 cells -- their first
+// kBinGroup places, one contiguous 2 KiB run of the bins -- is brought into
+// shared memory by a bulk copy, double-buffered per warp: the copy for the
+// warp's next task is started before the current task's rounds, so the
+// copy engine moves it while the warp works and the rounds read the first
+// places of every cell (most cells hold at most kBinGroup records) from
+// shared memory.  Places beyond the first group are read from global
+// memory.
+template <bool kHasBim, bool kBinned, bool kSingle, bool kStage>
 __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
-  __shared__ uint4 s_cells[8][32];  // per non-empty cell of the task: key, first slot, records, offset
-  __shared__ VisitQueue s_visit[kHasBim ? 8 : 1];
+  // per non-empty cell of the task: (key, first slot) and (records | offset << 8)
+  __shared__ uint2 s_cell[8][32];
+  __shared__ uint32_t s_noff[8][32];
+  __shared__ FaceQueue s_face[kHasBim ? 8 : 1];
   __shared__ float s_maxr[kSingle ? kCtxSpecies : 1];
+  __shared__ __align__(128) float4 s_stage[kStage ? 8 : 1][kStage ? 2 : 1][kStage ? 32 * kBinGroup : 1];
+  __shared__ uint64_t s_bar[kStage ? 8 : 1][2];
   if (kSingle) {  // before any warp may leave: one barrier for the whole CTA
     for (uint32_t t = threadIdx.x; t < p.S; t += blockDim.x) s_maxr[t] = p.species[p.inst0.block * p.S + t].max_r;
     __syncthreads();
@@ -1053,15 +1160,35 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   const uint32_t n_tasks = (p.n_cells + 31u) >> 5;
   const uint32_t nw = gridDim.x * (blockDim.x >> 5);
   const uint32_t le_mask = lane == 31 ? kFull : ((2u << lane) - 1u);
-  VisitQueue& vqueue = s_visit[kHasBim ? warp : 0];
-  uint32_t vq = 0;  // queued visits (warp-uniform)
+  FaceQueue& fqueue = s_face[kHasBim ? warp : 0];
+  uint32_t fq = 0;  // queued records (warp-uniform)
+  const uint32_t tk0 = blockIdx.x * (blockDim.x >> 5) + warp;
+  // group 0 of task `task` into stage buffer b (lane 0)
+  auto stage = [&](uint32_t task, uint32_t b) {
+    const uint32_t first = task * 32u, cells = min(32u, p.n_cells - first);
+    bulk_to_smem(&s_stage[kStage ? warp : 0][kStage ? b : 0][0], p.bins + bin_index(p, first, 0),
+                 cells * kBinGroup * (uint32_t)sizeof(float4), &s_bar[kStage ? warp : 0][b]);
+  };
+  uint32_t phase = 0;  // bit b: parity of stage buffer b's next completion
+  if (kStage) {
+    if (lane == 0) {
+      mbar_init(&s_bar[warp][0]);
+      mbar_init(&s_bar[warp][1]);
+      mbar_init_fence();
+      if (tk0 < n_tasks) stage(n_tasks - 1u - tk0, 0);
+    }
+    __syncwarp();
+  }
   // Cells are taken from the highest key down: the bins written last by
   // k_bin (its records stream in ascending cell order) are still in L2,
   // and the next state's low slots, written last here, are the first the
   // next step's k_bin reads.
-  for (uint32_t tk = blockIdx.x * (blockDim.x >> 5) + warp; tk < n_tasks; tk += nw) {
+  uint32_t it = 0;
+  for (uint32_t tk = tk0; tk < n_tasks; tk += nw, ++it) {
     const uint32_t task = n_tasks - 1u - tk;
     const uint32_t cell = task * 32u + lane;
+    const uint32_t buf = it & 1u;
+    if (kStage && lane == 0 && tk + nw < n_tasks) stage(n_tasks - 1u - (tk + nw), buf ^ 1u);
     uint32_t cs = 0, n = 0;
     if (cell < p.n_cells) {
       cs = __ldg(&p.cell_start[cell]);
@@ -1082,20 +1209,33 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
       if (lane >= (uint32_t)d) incl += t;
     }
     const uint32_t off = incl - n, total = __shfl_sync(kFull, incl, 31);
-    if (n > 0) s_cells[warp][q] = make_uint4(cell, cs, n, off);
+    if (n > 0) {
+      s_cell[warp][q] = make_uint2(cell, cs);
+      s_noff[warp][q] = n | (off << 8);
+    }
     __syncwarp();
+    if (kStage) {
+      if (!mbar_wait(&s_bar[warp][buf], (phase >> buf) & 1u)) {
+        if (lane == 0) atomicOr(&c->status, kStatTimeout);
+        return;
+      }
+      phase ^= 1u << buf;
+    }
+    const float4* stage_base = &s_stage[kStage ? warp : 0][kStage ? buf : 0][0];
     uint32_t before = 0;  // non-empty cells that start before this round
     for (uint32_t rb = 0; rb < total; rb += 32u) {
       const uint32_t M = __reduce_or_sync(kFull, (n > 0 && off >= rb && off - rb < 32u) ? 1u << (off - rb) : 0u);
       const uint32_t t = rb + lane;
-      uint32_t nbm = 0, key0 = 0, ca = 0;  // forward cells to visit from this lane's record
+      bool near = false;  // this lane's record may have partners in forward neighbour cells
+      uint32_t ca = 0;
       float4 ra = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (t < total) {
         const uint32_t oq = before + __popc(M & le_mask) - 1u;
-        const uint4 cc = s_cells[warp][oq];
-        const uint32_t ocell = cc.x, ocs = cc.y, on = cc.z;
-        const uint32_t j = t - cc.w;
-        const CellView cb = cell_records<kBinned>(p, ocell, ocs);
+        const uint2 cc = s_cell[warp][oq];
+        const uint32_t no = s_noff[warp][oq];
+        const uint32_t ocell = cc.x, ocs = cc.y, on = no & 0xFFu;
+        const uint32_t j = t - (no >> 8);
+        const BinView<kStage> cb{stage_base + (ocell - task * 32u) * kBinGroup, cell_records<kBinned>(p, ocell, ocs)};
         ra = cb.ldg(j);
         Seeker k;
         const bool search = kHasBim && seeker_init<kSingle>(p, ra, k, kSingle ? s_maxr : nullptr, adv0);
@@ -1145,43 +1285,28 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
             const int32_t bb = pair_reaction(p, k, qm);
             if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
           }
-          nbm = forward_mask<kSingle>(p, k, &key0);
+          near = near_forward_face<kSingle>(p, k);
         }
       }
       if (kHasBim) {
-        // queue one visit per marked neighbour cell, draining 32 at a time
-        const DevInstance& I = inst_of<kSingle>(p, kSingle ? 0u : rec_w(ra) >> 16);
-        while (__any_sync(kFull, nbm != 0u)) {
-          const bool has = nbm != 0u;
-          uint32_t nkey = 0;
-          if (has) {
-            nkey = forward_key(key0, (uint32_t)(__ffs(nbm) - 1), I.dims[0], I.dims[1]);
-            nbm &= nbm - 1u;
-          }
-          const uint32_t ball = __ballot_sync(kFull, has);
-          if (has) {
-            const uint32_t pos = vq + __popc(ball & ((1u << lane) - 1u));
-            vqueue.rec[pos] = ra;
-            vqueue.ca[pos] = ca;
-            vqueue.key[pos] = nkey;
-          }
-          vq += __popc(ball);
-          if (vq >= 32u) {
-            drain_visits<kBinned, kSingle>(p, c, vqueue, vq, kSingle ? s_maxr : nullptr, adv0);
-            vq -= 32u;
-          }
+        // records near a +face into the warp's queue, visited 32 at a time
+        const uint32_t ball = __ballot_sync(kFull, near);
+        if (near) {
+          const uint32_t pos = fq + __popc(ball & ((1u << lane) - 1u));
+          fqueue.rec[pos] = ra;
+          fqueue.ca[pos] = ca;
+        }
+        fq += __popc(ball);
+        if (fq >= 32u) {
+          drain_faces<kBinned, kSingle>(p, c, fqueue, fq, kSingle ? s_maxr : nullptr, adv0);
+          fq -= 32u;
         }
       }
       before += __popc(M);
     }
     __syncwarp();
   }
-  if (kHasBim) {
-    __syncwarp();
-    if (lane < vq)
-      visit_neighbour<kBinned, kSingle>(p, c, vqueue.rec[lane], vqueue.ca[lane], vqueue.key[lane],
-                                        kSingle ? s_maxr : nullptr, adv0);
-  }
+  if (kHasBim && fq > 0) drain_faces<kBinned, kSingle>(p, c, fqueue, fq, kSingle ? s_maxr : nullptr, adv0);
 }
 
 constexpr uint32_t kBigChunk = 2048;  // records sorted per shared-memory pass
@@ -1439,7 +1564,7 @@ __device__ __forceinline__ void commit_events(const KParams& p) {
 // end's smallest undecided partner is the other end.
 template <bool kSurf>
 __global__ void __launch_bounds__(1024) k_match(KParams p) {
-  __shared__ uint32_t s_more, s_deaths;
+  __shared__ uint32_t s_next[2], s_deaths;
   DevCtrl* c = p.ctrl;
   if (ld_u32(&c->status)) return;
   // read before the barriers below; thread 0 advances it at the end
@@ -1454,37 +1579,95 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
   DevPair* pr = p.pairs;
   if (threadIdx.x == 0) s_deaths = 0;
 
-  for (uint32_t round = 0; round <= K; ++round) {
-    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
-      if (pr[k].state == 0) {
-        atomicMin(&p.best[pr[k].i], pr[k].j);
-        atomicMin(&p.best[pr[k].j], pr[k].i);
+  // Rounds of locally dominant pairs.  In round r a pending pair (i, j)
+  // offers tag(r) | j to best[i] and tag(r) | i to best[j] (atomicMin); the
+  // pairs that are each other's minimum are matched (best = 0 at both
+  // ends), and a pending pair with a matched end is dropped in the next
+  // round.  tag(r) falls with r, so values of earlier rounds lose every
+  // minimum and best needs no reset between rounds: two passes and two
+  // barriers per round.  The pairs still pending are compacted, with their
+  // ends, into one of two lists for the next round.  Each round matches the smallest
+  // pending pair at least, so there are at most K rounds; the result is the
+  // greedy matching in (lower slot, upper slot) order.
+  unsigned long long* best = p.best;
+  uint4* lists[2] = {p.match_list, p.match_list + p.pair_cap};
+  if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
+  __syncthreads();
+  // Each thread takes kMatchIlp list entries at a time, so that their
+  // loads (entry, then the two matcher words) are in flight together.
+  constexpr uint32_t kMatchIlp = 4;
+  uint32_t n_pend = K;
+  for (uint32_t round = 0; n_pend > 0 && round <= K; ++round) {
+    const uint4* in = round == 0 ? nullptr : lists[(round - 1) & 1];
+    uint4* out = lists[round & 1];
+    const unsigned long long tag = (unsigned long long)(0xFFFFFFFFu - round) << 32;
+    const uint32_t span = blockDim.x * kMatchIlp;
+    // pass A: offers, except from pairs with an end matched in an earlier round
+    for (uint32_t e0 = threadIdx.x; e0 < n_pend; e0 += span) {
+      uint4 ent[kMatchIlp];
+      unsigned long long bi[kMatchIlp], bj[kMatchIlp];
+#pragma unroll
+      for (uint32_t u = 0; u < kMatchIlp; ++u) {
+        const uint32_t e = e0 + u * blockDim.x;
+        if (e < n_pend) ent[u] = in ? in[e] : make_uint4(e, pr[e].i, pr[e].j, 0u);
       }
-    __syncthreads();
-    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
-      if (pr[k].state == 0 && ld_u32(&p.best[pr[k].i]) == pr[k].j && ld_u32(&p.best[pr[k].j]) == pr[k].i)
-        pr[k].state = 3;
-    __syncthreads();
-    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
-      if (pr[k].state == 3) {
-        atomicExch(&p.best[pr[k].i], kMatched);
-        atomicExch(&p.best[pr[k].j], kMatched);
-        pr[k].state = 1;
+#pragma unroll
+      for (uint32_t u = 0; u < kMatchIlp; ++u) {
+        bi[u] = bj[u] = kFree64;
+        if (round > 0 && e0 + u * blockDim.x < n_pend) {
+          bi[u] = __ldcg(&best[ent[u].y]);
+          bj[u] = __ldcg(&best[ent[u].z]);
+        }
       }
+#pragma unroll
+      for (uint32_t u = 0; u < kMatchIlp; ++u)
+        if (e0 + u * blockDim.x < n_pend && bi[u] != 0ull && bj[u] != 0ull) {
+          atomicMin(&best[ent[u].y], tag | ent[u].z);
+          atomicMin(&best[ent[u].z], tag | ent[u].y);
+        }
+    }
     __syncthreads();
-    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
-      if (pr[k].state == 0 && (ld_u32(&p.best[pr[k].i]) == kMatched || ld_u32(&p.best[pr[k].j]) == kMatched))
-        pr[k].state = 2;
-    if (threadIdx.x == 0) s_more = 0;
-    __syncthreads();
-    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
-      if (pr[k].state == 0) {
-        atomicExch(&p.best[pr[k].i], kFree);
-        atomicExch(&p.best[pr[k].j], kFree);
-        s_more = 1;
+    // pass B: match mutual minima, drop pairs with a matched end, keep the rest
+    for (uint32_t e0 = 0; e0 < n_pend; e0 += span) {
+      uint4 ent[kMatchIlp];
+      unsigned long long bi[kMatchIlp], bj[kMatchIlp];
+#pragma unroll
+      for (uint32_t u = 0; u < kMatchIlp; ++u) {
+        const uint32_t e = e0 + u * blockDim.x + threadIdx.x;
+        if (e < n_pend) ent[u] = in ? in[e] : make_uint4(e, pr[e].i, pr[e].j, 0u);
       }
+#pragma unroll
+      for (uint32_t u = 0; u < kMatchIlp; ++u)
+        if (e0 + u * blockDim.x + threadIdx.x < n_pend) {
+          bi[u] = __ldcg(&best[ent[u].y]);
+          bj[u] = __ldcg(&best[ent[u].z]);
+        }
+#pragma unroll
+      for (uint32_t u = 0; u < kMatchIlp; ++u) {
+        bool keep = false;
+        if (e0 + u * blockDim.x + threadIdx.x < n_pend) {
+          if (bi[u] == (tag | ent[u].z) && bj[u] == (tag | ent[u].y)) {
+            best[ent[u].y] = 0ull;
+            best[ent[u].z] = 0ull;
+            pr[ent[u].x].state = 1;
+          } else if (bi[u] == 0ull || bj[u] == 0ull) {
+            pr[ent[u].x].state = 2;
+          } else {
+            keep = true;
+          }
+        }
+        // survivors to the next list, one shared-memory atomic per warp
+        const uint32_t ball = __ballot_sync(kFull, keep);
+        uint32_t base = 0;
+        if (ball && lane_id() == 0) base = atomicAdd(&s_next[round & 1], (uint32_t)__popc(ball));
+        base = __shfl_sync(kFull, base, 0);
+        if (keep) out[base + __popc(ball & ((1u << lane_id()) - 1u))] = ent[u];
+      }
+    }
     __syncthreads();
-    if (!s_more) break;
+    n_pend = s_next[round & 1];
+    if (threadIdx.x == 0) s_next[(round + 1) & 1] = 0;
+    __syncthreads();
   }
 
   // products: at the D-weighted reaction point, displaced along a random
@@ -1546,8 +1729,8 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
   }
   __syncthreads();
   for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
-    atomicExch(&p.best[pr[k].i], kFree);
-    atomicExch(&p.best[pr[k].j], kFree);
+    best[pr[k].i] = kFree64;
+    best[pr[k].j] = kFree64;
   }
   commit_events(p);
   for (uint32_t t = threadIdx.x; t < p.n_tiles; t += blockDim.x) p.scan_flags[t] = 0ull;
@@ -1656,6 +1839,64 @@ __global__ void __launch_bounds__(256) k_species_counts(KParams p, unsigned long
   }
 }
 
+// Squared diffusion moves of the coming step, summed per (instance,
+// species): the step's own Philox counters, normals and wall reflections
+// (advance_rec, before its reactions), read only.  An observable
+// (bd_measure_msd), launched before a step, not part of it.  Sums go
+// through shared memory when the (instance, species) table fits.
+constexpr uint32_t kMsdShared = 512;
+
+template <bool kTable>
+__global__ void __launch_bounds__(256) k_msd(KParams p, double* sum, unsigned long long* cnt) {
+  __shared__ double s_sum[kMsdShared];
+  __shared__ unsigned long long s_cnt[kMsdShared];
+  const DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;  // the step will not run: nothing to measure
+  const uint32_t keys = p.n_inst * p.S;
+  const bool in_smem = keys <= kMsdShared;
+  if (in_smem)
+    for (uint32_t k = threadIdx.x; k < keys; k += blockDim.x) {
+      s_sum[k] = 0.0;
+      s_cnt[k] = 0ull;
+    }
+  __syncthreads();
+  const uint32_t cur = ld_u32(&c->cur);
+  const float4* st = cur_state(p, cur);
+  const uint32_t n = ld_u32(&c->n_slots);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 rec = st[i];
+    const uint32_t w = rec_w(rec);
+    if (w == kDead) continue;
+    const uint32_t inst = w >> 16, sp = w & kSpeciesMask;
+    if (!advancing(p.inst_flags[inst])) continue;
+    const DevInstance& I = p.inst[inst];
+    const uint32_t local = i - p.inst_slot_base[inst];
+    const float sigma = p.species[I.block * p.S + sp].sigma;
+    const U4 rn = philox(U4{local, p.inst_step[inst], kTagDiffuse, 0u}, I.key_lo, I.key_hi);
+    float g0, g1, g2;
+    normals3<kTable>(rn, p.gauss, g0, g1, g2);
+    const double dx = (double)reflect(__fmaf_rn(sigma, g0, rec.x), I.lo[0], I.hi[0]) - rec.x;
+    const double dy = (double)reflect(__fmaf_rn(sigma, g1, rec.y), I.lo[1], I.hi[1]) - rec.y;
+    const double dz = (double)reflect(__fmaf_rn(sigma, g2, rec.z), I.lo[2], I.hi[2]) - rec.z;
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const uint32_t key = inst * p.S + sp;
+    if (in_smem) {
+      atomicAdd(&s_sum[key], d2);
+      atomicAdd(&s_cnt[key], 1ull);
+    } else {
+      atomicAdd(&sum[key], d2);
+      atomicAdd(&cnt[key], 1ull);
+    }
+  }
+  __syncthreads();
+  if (in_smem)
+    for (uint32_t k = threadIdx.x; k < keys; k += blockDim.x)
+      if (s_cnt[k]) {
+        atomicAdd(&sum[k], s_sum[k]);
+        atomicAdd(&cnt[k], s_cnt[k]);
+      }
+}
+
 }  // namespace
 
 int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
@@ -1711,14 +1952,14 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     if (p.n_panels) BD_STREAM_LAUNCH3(KERNEL, 1, 1); \
     else BD_STREAM_LAUNCH(KERNEL, 0);             \
   } while (0)
-#define BD_PAIRS_LAUNCH(BINNED)                                                                      \
+#define BD_PAIRS_LAUNCH(BINNED, STAGE)                                                               \
   do {                                                                                               \
     if (single) {                                                                                    \
-      if (has_bim) k_pairs_cells<true, BINNED, true><<<shape.grid_pairs, 256, 0, s>>>(p);       \
-      else k_pairs_cells<false, BINNED, true><<<shape.grid_pairs, 256, 0, s>>>(p);              \
+      if (has_bim) k_pairs_cells<true, BINNED, true, STAGE><<<shape.grid_pairs, 256, 0, s>>>(p);  \
+      else k_pairs_cells<false, BINNED, true, STAGE><<<shape.grid_pairs, 256, 0, s>>>(p);         \
     } else {                                                                                         \
-      if (has_bim) k_pairs_cells<true, BINNED, false><<<shape.grid_pairs, 256, 0, s>>>(p);      \
-      else k_pairs_cells<false, BINNED, false><<<shape.grid_pairs, 256, 0, s>>>(p);             \
+      if (has_bim) k_pairs_cells<true, BINNED, false, STAGE><<<shape.grid_pairs, 256, 0, s>>>(p); \
+      else k_pairs_cells<false, BINNED, false, STAGE><<<shape.grid_pairs, 256, 0, s>>>(p);        \
     }                                                                                                \
   } while (0)
   const bool single = p.n_inst == 1 && p.S <= kCtxSpecies && p.U <= kCtxUni;
@@ -1740,7 +1981,7 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     }
     k_scan<<<p.n_tiles, 1024, 0, s>>>(p);
     done("k_scan");
-    BD_PAIRS_LAUNCH(true);
+    BD_PAIRS_LAUNCH(true, kStagePairs);
     done("k_pairs_cells");
     k_pairs_big_sort<true><<<kBigGrid, 256, 0, s>>>(p);
     done("k_pairs_big_sort");
@@ -1759,12 +2000,12 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   done("k_scan");
   BD_STREAM_LAUNCH_COMPACT(k_scatter);
   done("k_scatter");
-  BD_PAIRS_LAUNCH(false);
+  BD_PAIRS_LAUNCH(false, false);
+  done("k_pairs_cells");
 #undef BD_STREAM_LAUNCH
 #undef BD_STREAM_LAUNCH_COMPACT
 #undef BD_STREAM_LAUNCH3
 #undef BD_PAIRS_LAUNCH
-  done("k_pairs_cells");
   k_pairs_big_sort<false><<<kBigGrid, 256, 0, s>>>(p);
   done("k_pairs_big_sort");
   if (has_bim) {
@@ -1783,6 +2024,11 @@ void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaS
 
 void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaStream_t s) {
   k_species_counts<<<152 * 4, 256, 0, s>>>(p, counts);
+}
+
+void enqueue_msd(const KParams& p, bool table, double* sum, unsigned long long* counts, cudaStream_t s) {
+  if (table) k_msd<true><<<152 * 4, 256, 0, s>>>(p, sum, counts);
+  else k_msd<false><<<152 * 4, 256, 0, s>>>(p, sum, counts);
 }
 
 }  // namespace bd

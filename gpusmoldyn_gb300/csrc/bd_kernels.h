@@ -34,7 +34,8 @@ struct KParams {
   unsigned long long* scan_flags; // [n_tiles] single-pass scan: state << 32 | sum, 0 between steps
   uint32_t scan_withhold;     // test switch: tile 0 of the scan does not publish (its successors time out)
   DevPair* pairs;             // [pair_cap]
-  uint32_t* best;             // [capacity] matcher scratch, all 0xFFFFFFFF between steps
+  unsigned long long* best;   // [capacity] matcher words, all ones between steps
+  uint4* match_list;          // [2 * pair_cap] pending pairs (index, ends) of the matcher's rounds
   unsigned long long* events; // [I * R] reaction event counters (committed steps)
   unsigned long long* pending;// [I * R] events of the step in flight, added at commit
   uint32_t n_inst, S, U, B, Z, R;
@@ -83,6 +84,9 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
 void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaStream_t stream);
 // Count live records per (instance, species): counts[I * S] must be zeroed.
 void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaStream_t stream);
+// Squared diffusion moves of the coming step per (instance, species), added
+// into sum / counts (bd_measure_msd).
+void enqueue_msd(const KParams& p, bool table, double* sum, unsigned long long* counts, cudaStream_t stream);
 
 // Tile size of the cell scan.
 constexpr uint32_t kScanTile = 16384;

@@ -121,3 +121,32 @@ class Server:
 
     def close(self):
         self.s.close()
+
+
+def run_sequential(jobs, make_request=c3_request, device=0, dt=1e-3, normals="boxmuller", density=2.0):
+    """The same requests served one at a time, in arrival order, on the wall
+    clock: each waits for the previous one to finish, then runs alone as a
+    plain system (handle, network, upload, its steps, readback) -- the
+    baseline that continuous batching is measured against."""
+    order = sorted(jobs, key=lambda j: j["arrival"])
+    lat = []
+    work = 0.0
+    t0 = time.perf_counter()
+    for job in order:
+        now = time.perf_counter() - t0
+        if job["arrival"] > now:
+            time.sleep(job["arrival"] - now)
+        desc, pos, sp, steps = job["payload"] if "payload" in job else make_request(job)
+        s = System(desc["box_lo"], desc["box_hi"], dt=dt, seed=desc["seed"], normals=normals, device=device)
+        c3_add_network(s, density)
+        s.finalize()
+        s.set_particles(pos, sp)
+        s.step(steps)
+        s.particles()
+        s.close()
+        lat.append(time.perf_counter() - t0 - job["arrival"])
+        work += float(job["n"] * job["steps"])
+    wall = time.perf_counter() - t0
+    lat = np.array(lat)
+    return dict(jobs=len(order), wall_s=wall, p50_s=float(np.percentile(lat, 50)),
+                p99_s=float(np.percentile(lat, 99)), mean_s=float(lat.mean()), particle_steps_per_s=work / wall)

@@ -295,6 +295,15 @@ class System:
         L.check(self.lib.bd_get_species_counts(self.h, instance, _ptr(out), self.n_species), "species_counts")
         return out[:self.n_species]
 
+    def measure_msd(self, nsteps, instance=-1):
+        """Take nsteps steps and return (msd, counts) per species: the mean
+        squared diffusion move per step (bd_measure_msd)."""
+        msd = np.zeros(max(self.n_species, 1), np.float64)
+        cnt = np.zeros(max(self.n_species, 1), np.uint64)
+        L.check(self.lib.bd_measure_msd(self.h, instance, int(nsteps), _ptr(msd), _ptr(cnt), self.n_species),
+                "bd_measure_msd")
+        return msd[:self.n_species], cnt[:self.n_species]
+
     def instance_counts(self) -> np.ndarray:
         out = np.zeros(self.n_instances, np.uint64)
         L.check(self.lib.bd_get_instance_counts(self.h, _ptr(out), self.n_instances), "instance_counts")

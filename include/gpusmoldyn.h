@@ -306,6 +306,17 @@ BD_API bd_status bd_set_ensemble_particles(bd_handle h, const float *xyz4, const
  * over instances (instance = -1) or for one instance.  Replaces reading
  * the whole type array back (particles.cpp:509-552 debug dumps). */
 BD_API bd_status bd_get_species_counts(bd_handle h, int instance, uint64_t *counts, int n);
+/* Mean squared displacement per species over the next nsteps steps, which
+ * are taken as bd_step takes them (synchronises).  msd[s] is the mean,
+ * over the moves of species s's particles (of one instance, or of all for
+ * instance = -1), of |x' - x|^2 with x' the position after the step's
+ * diffusion move and the wall reflections, before the step's reactions;
+ * counts[s] is the number of moves averaged.  In the bulk it equals
+ * 6 D dt.  The moves are recomputed from each step's own random counters
+ * by a read-only kernel launched before the step.  Handles with surface
+ * panels return BD_ERR_UNSUPPORTED.  Replaces watching the particles move
+ * in the viewer (particles.cpp:254-275, render_particles.cpp). */
+BD_API bd_status bd_measure_msd(bd_handle h, int instance, int nsteps, double *msd, uint64_t *counts, int n);
 
 /* Live counts per instance (synchronises). */
 BD_API bd_status bd_get_instance_counts(bd_handle h, uint64_t *counts, int n_instances);

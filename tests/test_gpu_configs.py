@@ -133,7 +133,7 @@ def brute_force_pairs(recs, radius2, n_species):
 @pytest.mark.parametrize("sort", SORTS)
 def test_c3_pair_search_misses_no_pair(sort):
     """The c3 network's six second-order reactions alone (no births, so no
-    record is excluded as a newborn), at 20x their rates, on a
+    record is excluded as a newborn), at 50x their rates, on a
     262,144-particle cube.  Every reaction has probability 1, so the greedy
     matching accepts each candidate pair whose two records are still free:
     after the step no two records that did not react may lie within their
@@ -148,7 +148,7 @@ def test_c3_pair_search_misses_no_pair(sort):
         s.add_species(float(d))
     for order, rc, pr, k in rx:
         if order == 2:
-            s.add_reaction(order, rc, pr, float(k) * 20.0)
+            s.add_reaction(order, rc, pr, float(k) * 50.0)
     s.finalize()
     pos, sp = configs.c3_particles(n, side)
     s.set_particles(pos, sp)
@@ -166,7 +166,7 @@ def test_c3_pair_search_misses_no_pair(sort):
         reacted = np.zeros(len(got), bool)
         reacted[acc[:, 0]] = True
         reacted[acc[:, 1]] = True
-        assert len(acc) > 500, len(acc)
+        assert len(acc) > 300, len(acc)
         # every candidate pair has a reacted end
         assert np.all(reacted[pairs[:, 0]] | reacted[pairs[:, 1]])
         recs = got.copy()

@@ -210,3 +210,110 @@ def test_competing_reactions_split_the_rate():
     k_theory = kstep / dt * (1 + 2 * (k / (4 * math.pi * Dsum)) / math.sqrt(math.pi * Dsum * T))
     k_meas = -math.log(na / n) / (T * n / side ** 3)
     assert k_meas / k_theory == pytest.approx(1.0, abs=0.01), (k_meas, k_theory)
+
+
+def test_ensemble_msd_per_instance_with_scaled_d():
+    """A batched ensemble (one pipeline per step over every instance): each
+    instance diffuses with its own D scale, and its MSD is 6 D d_scale t
+    within 1%.  All particles of an instance start at its box centre, so
+    |x - centre|^2 needs no identity."""
+    n, steps, dt = 300_000, 40, 1e-3
+    scales = [0.5, 1.0, 2.0, 3.0]
+    inst = [dict(box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0), seed=300 + k, d_scale=d, k2_scale=1.0)
+            for k, d in enumerate(scales)]
+    s = System(dt=dt, seed=30, instances=inst)
+    s.add_species(1.0)
+    s.add_species(0.4)
+    s.add_reaction(2, [0, 1], [0], 1e-9)  # a second-order reaction that never fires
+    s.finalize()
+    pos = np.full((n * len(scales), 3), 100.0, np.float32)
+    sp = (np.arange(n * len(scales)) % 2).astype(np.int32)
+    s.set_ensemble_particles(pos, sp, [n] * len(scales))
+    s.step(steps)
+    s.synchronize()
+    for k, d in enumerate(scales):
+        p, q = s.particles(k)
+        r2 = np.sum((p.astype(np.float64) - 100.0) ** 2, axis=1)
+        for species, D in ((0, 1.0), (1, 0.4)):
+            ratio = r2[q == species].mean() / (6 * D * d * dt * steps)
+            # relative standard error sqrt(2/3 / 1.5e5) = 0.2%; tolerance 1%
+            assert ratio == pytest.approx(1.0, abs=0.01), (k, species, ratio)
+    s.close()
+
+
+def test_ensemble_equilibrium_per_instance_with_scaled_kon():
+    """Three instances of A + B <-> C at the c2 density (k_off 10 /s, pgemmax
+    0.2) with k_on scaled 0.5, 1 and 2 from 0.05 um^3/s, in one pipeline:
+    each instance's time-averaged C count equals its own mass-action
+    solution c = (k_on k2_scale / k_off) (A0 - c)(B0 - c) / V within 1%."""
+    n0, dens, dt = 150_000, 1_000_000 / 60.0 ** 3, 5e-4
+    side = float((2 * n0 / dens) ** (1 / 3))
+    V = side ** 3
+    scales = [0.5, 1.0, 2.0]
+    inst = [dict(box_lo=(0.0, 0.0, 0.0), box_hi=(side,) * 3, seed=310 + k, d_scale=1.0, k2_scale=ks)
+            for k, ks in enumerate(scales)]
+    s = System(dt=dt, seed=31, instances=inst)
+    A, B, Cc = s.add_species(1.0), s.add_species(1.0), s.add_species(0.5)
+    s.add_reaction(2, [A, B], [Cc], 0.05)
+    back = s.add_reaction(1, [Cc], [A, B], 10.0)
+    s.set_product_placement(back, L.BD_PP_PGEMMAX, 0.2)
+    s.finalize()
+    g = rng(31)
+    pos = np.concatenate([uniform_positions(g, 2 * n0, (0, 0, 0), (side,) * 3) for _ in scales])
+    sp = np.tile(np.concatenate([np.zeros(n0), np.ones(n0)]).astype(np.int32), len(scales))
+    s.set_ensemble_particles(pos, sp, [2 * n0] * len(scales))
+    s.step(3000)  # ~15 relaxation times
+    samples = [[] for _ in scales]
+    for _ in range(400):
+        s.step(20)
+        for k in range(len(scales)):
+            samples[k].append(int(s.species_counts(k)[Cc]))
+    for k, ks in enumerate(scales):
+        c_mean = float(np.mean(samples[k]))
+        K = 0.05 * ks / 10.0
+        qa, qb, qc = K / V, -(2 * K * n0 / V + 1), K * n0 * n0 / V
+        c_theory = (-qb - math.sqrt(qb * qb - 4 * qa * qc)) / (2 * qa)
+        assert c_mean / c_theory == pytest.approx(1.0, abs=0.01), (k, ks, c_mean, c_theory)
+    s.close()
+
+
+@pytest.mark.parametrize("normals,var", [("boxmuller", 1.0), ("table", 0.99968)])
+def test_msd_observable_equals_6_d_dt(normals, var):
+    """bd_measure_msd: the mean squared diffusion move per step of each
+    species is 6 D dt (times the table's variance in table mode) within 1%,
+    in a box so large that walls reflect almost nothing; every live
+    particle's move is counted once per step; the steps are taken."""
+    n, steps, dt = 400_000, 10, 1e-3
+    s = System((0, 0, 0), (500.0,) * 3, dt=dt, seed=41, normals=normals)
+    s.add_species(1.5)
+    s.add_species(0.2)
+    s.add_reaction(2, [0, 1], [0], 1e-9)
+    s.finalize()
+    g = rng(41)
+    s.set_particles(uniform_positions(g, n, (100.0,) * 3, (400.0,) * 3), (np.arange(n) % 2).astype(np.int32))
+    step0 = s.step_count()
+    msd, cnt = s.measure_msd(steps)
+    assert s.step_count() == step0 + steps
+    np.testing.assert_array_equal(cnt, [steps * n // 2, steps * n // 2])
+    for species, D in ((0, 1.5), (1, 0.2)):
+        assert msd[species] / (6 * D * dt * var) == pytest.approx(1.0, abs=0.01), (species, msd[species])
+    s.close()
+
+
+def test_msd_observable_per_instance():
+    scales = [0.5, 2.0]
+    inst = [dict(box_lo=(0.0,) * 3, box_hi=(300.0,) * 3, seed=420 + k, d_scale=d, k2_scale=1.0)
+            for k, d in enumerate(scales)]
+    s = System(dt=1e-3, seed=42, instances=inst)
+    s.add_species(1.0)
+    s.add_reaction(2, [0, 0], [0], 1e-9)
+    s.finalize()
+    n = 200_000
+    g = rng(42)
+    pos = np.concatenate([uniform_positions(g, n, (50.0,) * 3, (250.0,) * 3) for _ in scales])
+    s.set_ensemble_particles(pos, np.zeros(2 * n, np.int32), [n, n])
+    for k, d in enumerate(scales):
+        msd, cnt = s.measure_msd(8, instance=k)
+        assert int(cnt[0]) == 8 * n
+        assert msd[0] / (6 * d * 1e-3) == pytest.approx(1.0, abs=0.01), (k, msd[0])
+    s.close()
