@@ -41,6 +41,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s plain vs batched ensemble on 1 GB300 at <1% rate/MSD error; p99"
+T_START = time.perf_counter()
+
+
+def progress(what):
+    """One line on stderr per bench section (stdout carries only the JSON)."""
+    print(f"[bench {time.perf_counter() - T_START:7.1f} s] {what}", file=sys.stderr, flush=True)
 UNIT = "particle-steps/s"
 
 
@@ -322,6 +328,7 @@ def run_gb300(args, dist):
         s.close()
         return None
     # ---------------- headline: device-timed plain step
+    progress("headline step")
     s, desc = build_workload(args.workload, args.n, device=device)
     s.step(args.warmup)
     s.synchronize()
@@ -380,6 +387,7 @@ def run_gb300(args, dist):
     }
 
     # ---------------- end to end through the C ABI with host buffers
+    progress('end to end through the C ABI with host buffers')
     if not args.no_e2e:
         s3, pos, sp = network_and_particles(args.workload, args.n, device)
         # the caller's arrays in the reference's layout (float4 positions, int
@@ -415,18 +423,22 @@ def run_gb300(args, dist):
         s3.close()
 
     # ---------------- the same step with surfaces (c3 inside a cell)
+    progress('the same step with surfaces')
     if not args.no_surfaces and args.workload == "c3":
         out["surfaces"] = run_surfaces(args, dist, device, out["value"])
 
     # ---------------- batched ensemble vs the plain per-instance loop
+    progress('batched ensemble vs the plain per-instance loop')
     if not args.no_batched:
         out["batched"] = run_batched(args, dist, device)
 
     # ---------------- serving: continuous batching of c5-style requests
+    progress('serving: continuous batching of c5-style requests')
     if not args.no_serving and dist.rank == 0:
         out["serving"] = run_serving(args, device)
 
     # ---------------- CPU baseline (rank 0, N = 1 only)
+    progress('CPU baseline')
     if not args.no_cpu and dist.rank == 0 and dist.world == 1:
         threads = os.cpu_count() or 1
         n = args.n or 16_000_000
@@ -507,7 +519,9 @@ def run_batched(args, dist, device):
         s.set_ensemble_particles(pos, sp, counts)
         return s
 
+    progress("batched: tuning on a scaled copy")
     tuned = tune.tune(lambda occ: build(mine[::8], occ), steps=20, warmup=5)
+    progress("batched: timed run")
     steps = max(args.steps, 2000)
     s = build(mine, tuned["occupancy"])
     s.set_launch_shape(*tuned["shape"])
@@ -524,6 +538,7 @@ def run_batched(args, dist, device):
     batched = dist.sum(steps * 0.5 * (n0 + n1)) / (ms_max / 1e3)
     s.close()
     # the same instances advanced one after another as plain systems
+    progress("batched: plain per-instance loop")
     loop_steps = 10
     total_ms = 0.0
     total_ps = 0.0
@@ -562,6 +577,7 @@ def run_serving(args, device):
     srv = Server(max_instances=64, hbm_budget=150e9, chunk=10, device=device)
     res = srv.run(jobs)
     srv.close()
+    progress("serving: one request at a time")
     seq = run_sequential(jobs, device=device)
     return {"workload": f"c5: {len(jobs)} requests, Poisson 50/s, N log-U[1e3, 5e6], steps U[100, 10000]",
             "p50_latency_s": res["p50_s"], "p99_latency_s": res["p99_s"], "mean_latency_s": res["mean_s"],
@@ -582,6 +598,7 @@ def main():
         else:
             out = run_gb300(args, dist)
         if out is not None and dist.rank == 0:
+            progress("done")
             print(json.dumps(out))
     finally:
         dist.close()

@@ -18,6 +18,7 @@ import time
 
 import numpy as np
 
+from . import _lib as L
 from .configs import c3_add_network, c3_network, c3_species, c3_steady_state, rng, uniform_positions
 from .system import System
 
@@ -74,11 +75,19 @@ class Server:
                 need = job["n"] * BYTES_PER_PARTICLE
                 if used + need > self.budget and active:
                     break
-                waiting.popleft()
                 ta = time.perf_counter()
                 desc, pos, sp, steps = job["payload"] if "payload" in job else make_request(job)
                 tb = time.perf_counter()
-                slot = s.admit(desc, pos, sp, steps)
+                try:
+                    slot = s.admit(desc, pos, sp, steps)
+                except L.BDError as e:
+                    # a slot harvested in this iteration is released by the
+                    # next step: admit again after it
+                    if e.code != L.BD_ERR_CAPACITY or not active:
+                        raise
+                    spent["admit"] += time.perf_counter() - tb
+                    break
+                waiting.popleft()
                 spent["make_request"] += tb - ta
                 spent["admit"] += time.perf_counter() - tb
                 job["admitted"] = time.perf_counter() - t0
