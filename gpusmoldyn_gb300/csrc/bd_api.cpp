@@ -365,6 +365,7 @@ bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int 
   h->shape.min_blocks = 4;
   h->shape.block_pairs = 256;
   h->shape.grid_pairs = h->n_sm * 8;
+  h->shape.grid_match = h->host_only ? 1 : match_grid(h->n_sm);
   memset(h->hctrl, 0, sizeof(DevCtrl));
   cudaMemset(h->ctrl.p, 0, sizeof(DevCtrl));
   *out = h;
@@ -1306,6 +1307,7 @@ BD_API bd_status bd_synchronize(bd_handle h) {
       c.scan_ticket = 0;
       c.surf_ticket = 0;
       c.n_virtual = 0;
+      c.bar_count = 0;
       st = push_ctrl(h);
       if (st) return st;
       st = build_graphs(h);

@@ -1557,42 +1557,71 @@ __device__ __forceinline__ void commit_events(const KParams& p) {
   }
 }
 
-// Resolve the candidate pairs into a matching, apply the reactions and
-// commit the step.  Each particle reacts at most once; the pairs accepted
-// are those of the greedy scan in (lower slot, upper slot) order, found in
-// parallel as rounds of locally dominant pairs: a pair is taken when each
-// end's smallest undecided partner is the other end.
-template <bool kSurf>
-__global__ void __launch_bounds__(1024) k_match(KParams p) {
-  __shared__ uint32_t s_next[2], s_deaths;
-  DevCtrl* c = p.ctrl;
-  if (ld_u32(&c->status)) return;
-  // read before the barriers below; thread 0 advances it at the end
-  const uint32_t step_now = (uint32_t)*(volatile uint64_t*)&c->step;
-  const uint32_t K = ld_u32(&c->n_pairs);
-  if (K > p.pair_cap) {
-    if (threadIdx.x == 0) atomicOr(&c->status, kStatPairs);
-    return;
-  }
-  const uint32_t cur = ld_u32(&c->cur);
-  float4* __restrict__ nx = next_state(p, cur);
-  DevPair* pr = p.pairs;
-  if (threadIdx.x == 0) s_deaths = 0;
+// Grid-wide barrier of a cooperative launch (every CTA resident): thread 0
+// of each CTA reads the generation, arrives on the counter, and either (the
+// last to arrive) resets the counter and advances the generation, or waits
+// for the generation to change.  The wait is bounded: after kGridSpins polls
+// the CTA raises kStatTimeout and the barrier returns false; the other CTAs
+// then run out at the same barrier or the next, so every CTA returns.
+constexpr uint32_t kGridSpins = 1u << 22;
 
-  // Rounds of locally dominant pairs.  In round r a pending pair (i, j)
-  // offers tag(r) | j to best[i] and tag(r) | i to best[j] (atomicMin); the
-  // pairs that are each other's minimum are matched (best = 0 at both
-  // ends), and a pending pair with a matched end is dropped in the next
-  // round.  tag(r) falls with r, so values of earlier rounds lose every
-  // minimum and best needs no reset between rounds: two passes and two
-  // barriers per round.  The pairs still pending are compacted, with their
-  // ends, into one of two lists for the next round.  Each round matches the smallest
-  // pending pair at least, so there are at most K rounds; the result is the
-  // greedy matching in (lower slot, upper slot) order.
+__device__ bool grid_barrier(DevCtrl* c) {
+  __shared__ uint32_t s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_ok = 1u;
+    const uint32_t gen = *(volatile uint32_t*)&c->bar_gen;
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1u) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      for (uint32_t spins = 0; *(volatile uint32_t*)&c->bar_gen == gen; ++spins) {
+        if (spins > kGridSpins) {
+          atomicOr(&c->status, kStatTimeout);
+          s_ok = 0u;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return s_ok != 0u;
+}
+
+// Candidate pairs above which the matching runs over the whole grid.
+constexpr uint32_t kMatchOneCta = 8192;
+
+// Rounds of locally dominant pairs over K candidates, by the threads of one
+// CTA (kGrid false: __syncthreads, counters in shared memory) or of the
+// whole cooperative grid (kGrid: grid barriers, counters in DevCtrl).
+//
+// In round r a pending pair (i, j) offers tag(r) | j to best[i] and
+// tag(r) | i to best[j] (atomicMin); the pairs that are each other's
+// minimum are matched (best = 0 at both ends), and a pending pair with a
+// matched end is dropped.  tag(r) falls with r, so values of earlier rounds
+// lose every minimum and best needs no reset between rounds: two passes and
+// two barriers per round.  The pairs still pending are compacted, with
+// their ends, into one of two lists for the next round.  Each round matches
+// the smallest pending pair at least, so there are at most K rounds; the
+// result is the greedy matching in (lower slot, upper slot) order.
+// False when a grid barrier ran out (kStatTimeout is set).
+template <bool kGrid>
+__device__ bool match_rounds(const KParams& p, DevCtrl* c, uint32_t K, uint32_t* next) {
+  DevPair* pr = p.pairs;
   unsigned long long* best = p.best;
   uint4* lists[2] = {p.match_list, p.match_list + p.pair_cap};
-  if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
-  __syncthreads();
+  const uint32_t tid = kGrid ? blockIdx.x * blockDim.x + threadIdx.x : threadIdx.x;
+  const uint32_t nthr = kGrid ? gridDim.x * blockDim.x : blockDim.x;
+  const uint32_t lane = lane_id();
+  auto sync = [&]() -> bool {
+    if (kGrid) return grid_barrier(c);
+    __syncthreads();
+    return true;
+  };
   // Each thread takes kMatchIlp list entries at a time, so that their
   // loads (entry, then the two matcher words) are in flight together.
   constexpr uint32_t kMatchIlp = 4;
@@ -1601,51 +1630,53 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     const uint4* in = round == 0 ? nullptr : lists[(round - 1) & 1];
     uint4* out = lists[round & 1];
     const unsigned long long tag = (unsigned long long)(0xFFFFFFFFu - round) << 32;
-    const uint32_t span = blockDim.x * kMatchIlp;
+    const uint32_t span = nthr * kMatchIlp;
     // pass A: offers, except from pairs with an end matched in an earlier round
-    for (uint32_t e0 = threadIdx.x; e0 < n_pend; e0 += span) {
+    for (uint32_t e0 = tid; e0 < n_pend; e0 += span) {
       uint4 ent[kMatchIlp];
       unsigned long long bi[kMatchIlp], bj[kMatchIlp];
 #pragma unroll
       for (uint32_t u = 0; u < kMatchIlp; ++u) {
-        const uint32_t e = e0 + u * blockDim.x;
+        const uint32_t e = e0 + u * nthr;
         if (e < n_pend) ent[u] = in ? in[e] : make_uint4(e, pr[e].i, pr[e].j, 0u);
       }
 #pragma unroll
       for (uint32_t u = 0; u < kMatchIlp; ++u) {
         bi[u] = bj[u] = kFree64;
-        if (round > 0 && e0 + u * blockDim.x < n_pend) {
+        if (round > 0 && e0 + u * nthr < n_pend) {
           bi[u] = __ldcg(&best[ent[u].y]);
           bj[u] = __ldcg(&best[ent[u].z]);
         }
       }
 #pragma unroll
       for (uint32_t u = 0; u < kMatchIlp; ++u)
-        if (e0 + u * blockDim.x < n_pend && bi[u] != 0ull && bj[u] != 0ull) {
+        if (e0 + u * nthr < n_pend && bi[u] != 0ull && bj[u] != 0ull) {
           atomicMin(&best[ent[u].y], tag | ent[u].z);
           atomicMin(&best[ent[u].z], tag | ent[u].y);
         }
     }
-    __syncthreads();
-    // pass B: match mutual minima, drop pairs with a matched end, keep the rest
-    for (uint32_t e0 = 0; e0 < n_pend; e0 += span) {
+    if (!sync()) return false;
+    // pass B: match mutual minima, drop pairs with a matched end, keep the
+    // rest (the loop runs over whole warps: the ballot needs every lane)
+    const uint32_t warp_first = tid - lane;
+    for (uint32_t e0 = warp_first; e0 < n_pend; e0 += span) {
       uint4 ent[kMatchIlp];
       unsigned long long bi[kMatchIlp], bj[kMatchIlp];
 #pragma unroll
       for (uint32_t u = 0; u < kMatchIlp; ++u) {
-        const uint32_t e = e0 + u * blockDim.x + threadIdx.x;
+        const uint32_t e = e0 + u * nthr + lane;
         if (e < n_pend) ent[u] = in ? in[e] : make_uint4(e, pr[e].i, pr[e].j, 0u);
       }
 #pragma unroll
       for (uint32_t u = 0; u < kMatchIlp; ++u)
-        if (e0 + u * blockDim.x + threadIdx.x < n_pend) {
+        if (e0 + u * nthr + lane < n_pend) {
           bi[u] = __ldcg(&best[ent[u].y]);
           bj[u] = __ldcg(&best[ent[u].z]);
         }
 #pragma unroll
       for (uint32_t u = 0; u < kMatchIlp; ++u) {
         bool keep = false;
-        if (e0 + u * blockDim.x + threadIdx.x < n_pend) {
+        if (e0 + u * nthr + lane < n_pend) {
           if (bi[u] == (tag | ent[u].z) && bj[u] == (tag | ent[u].y)) {
             best[ent[u].y] = 0ull;
             best[ent[u].z] = 0ull;
@@ -1656,23 +1687,69 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
             keep = true;
           }
         }
-        // survivors to the next list, one shared-memory atomic per warp
+        // survivors to the next list, one atomic per warp
         const uint32_t ball = __ballot_sync(kFull, keep);
         uint32_t base = 0;
-        if (ball && lane_id() == 0) base = atomicAdd(&s_next[round & 1], (uint32_t)__popc(ball));
+        if (ball && lane == 0) base = atomicAdd(&next[round & 1], (uint32_t)__popc(ball));
         base = __shfl_sync(kFull, base, 0);
-        if (keep) out[base + __popc(ball & ((1u << lane_id()) - 1u))] = ent[u];
+        if (keep) out[base + __popc(ball & ((1u << lane) - 1u))] = ent[u];
       }
     }
-    __syncthreads();
-    n_pend = s_next[round & 1];
-    if (threadIdx.x == 0) s_next[(round + 1) & 1] = 0;
-    __syncthreads();
+    if (!sync()) return false;
+    n_pend = kGrid ? *(volatile uint32_t*)&next[round & 1] : next[round & 1];
+    // The other counter was last read before this round's first barrier,
+    // and the next round appends to it only after its own first barrier;
+    // this round's counter is reset only after the next round's second
+    // barrier, when every thread has read it.  No third barrier is needed.
+    if (tid == 0) next[(round + 1) & 1] = 0;
   }
+  return true;
+}
+
+// Resolve the candidate pairs into a matching, apply the reactions and
+// commit the step.  Each particle reacts at most once; the pairs accepted
+// are those of the greedy scan in (lower slot, upper slot) order, found in
+// parallel as rounds of locally dominant pairs (match_rounds).  Launched
+// cooperatively over the grid: with at most kMatchOneCta candidates (most
+// steps) CTA 0 does everything and the other CTAs leave at once; with more,
+// every CTA takes part in the rounds and the products, and CTA 0 commits.
+template <bool kSurf>
+__global__ void __launch_bounds__(1024) k_match(KParams p) {
+  __shared__ uint32_t s_next[2], s_deaths;
+  DevCtrl* c = p.ctrl;
+  if (ld_u32(&c->status)) return;
+  // read before the barriers below; thread 0 of CTA 0 advances it at the end
+  const uint32_t step_now = (uint32_t)*(volatile uint64_t*)&c->step;
+  const uint32_t K = ld_u32(&c->n_pairs);
+  if (K > p.pair_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&c->status, kStatPairs);
+    return;
+  }
+  const bool grid = gridDim.x > 1 && K > kMatchOneCta;  // the same in every CTA
+  if (!grid && blockIdx.x != 0) return;
+  const uint32_t cur = ld_u32(&c->cur);
+  float4* __restrict__ nx = next_state(p, cur);
+  DevPair* pr = p.pairs;
+  unsigned long long* best = p.best;
+  if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_deaths = 0;
+  if (grid) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      c->match_next[0] = c->match_next[1] = 0;
+      c->match_deaths = 0;
+    }
+    if (!grid_barrier(c)) return;
+    if (!match_rounds<true>(p, c, K, c->match_next)) return;
+  } else {
+    __syncthreads();
+    match_rounds<false>(p, c, K, s_next);
+  }
+  const uint32_t tid = grid ? blockIdx.x * blockDim.x + threadIdx.x : threadIdx.x;
+  const uint32_t nthr = grid ? gridDim.x * blockDim.x : blockDim.x;
 
   // products: at the D-weighted reaction point, displaced along a random
   // direction when the reaction has an unbinding radius
-  for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+  for (uint32_t k = tid; k < K; k += nthr) {
     const DevPair q = pr[k];
     if (q.state != 1) continue;
     const uint32_t inst = q.b >> 16;
@@ -1727,10 +1804,18 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     atomicAdd(&p.pending[(size_t)inst * p.R + br.rxn], 1ull);
     if (dead) atomicAdd(&s_deaths, dead);
   }
-  __syncthreads();
-  for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+  for (uint32_t k = tid; k < K; k += nthr) {
     best[pr[k].i] = kFree64;
     best[pr[k].j] = kFree64;
+  }
+  __syncthreads();
+  if (grid) {
+    // every CTA's products and deaths are in before CTA 0 commits
+    if (threadIdx.x == 0 && s_deaths) atomicAdd(&c->match_deaths, s_deaths);
+    if (!grid_barrier(c)) return;
+    if (blockIdx.x != 0) return;
+    if (threadIdx.x == 0) s_deaths = *(volatile uint32_t*)&c->match_deaths;
+    __syncthreads();
   }
   commit_events(p);
   for (uint32_t t = threadIdx.x; t < p.n_tiles; t += blockDim.x) p.scan_flags[t] = 0ull;
@@ -1899,6 +1984,23 @@ __global__ void __launch_bounds__(256) k_msd(KParams p, double* sum, unsigned lo
 
 }  // namespace
 
+// The matcher, cooperatively over shape.grid_match CTAs (all resident, so
+// its grid barriers cannot wait on a CTA that never runs).
+void launch_match(const KParams& p, const LaunchShape& shape, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(shape.grid_match > 1 ? shape.grid_match : 1));
+  cfg.blockDim = dim3(1024);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = shape.grid_match > 1 ? 1 : 0;
+  if (p.n_panels) cudaLaunchKernelEx(&cfg, k_match<true>, p);
+  else cudaLaunchKernelEx(&cfg, k_match<false>, p);
+}
+
 int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
                  const LaunchShape& shape, cudaStream_t s, StageHook hook, void* ctx) {
   (void)has_uni;
@@ -1989,8 +2091,7 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
       k_pairs_big_pairs<true, true><<<kBigGrid, 256, 0, s>>>(p);
       done("k_pairs_big_pairs");
     }
-    if (p.n_panels) k_match<true><<<1, 1024, 0, s>>>(p);
-    else k_match<false><<<1, 1024, 0, s>>>(p);
+    launch_match(p, shape, s);
     done("k_match");
     return n;
   }
@@ -2012,14 +2113,30 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
     k_pairs_big_pairs<true, false><<<kBigGrid, 256, 0, s>>>(p);
     done("k_pairs_big_pairs");
   }
-  if (p.n_panels) k_match<true><<<1, 1024, 0, s>>>(p);
-  else k_match<false><<<1, 1024, 0, s>>>(p);
+  launch_match(p, shape, s);
   done("k_match");
   return n;
 }
 
 void enqueue_instance_counts(const KParams& p, unsigned long long* counts, cudaStream_t s) {
   k_instance_counts<<<152 * 4, 256, 0, s>>>(p, counts);
+}
+
+// At most kMatchGrid CTAs: on the dense smoke step (24,509 candidates, 119
+// rounds) 32 CTAs took 0.985 ms against 1.06 ms for 152 (one per SM) and
+// 1.07 ms for 16, and a grid launch costs the small-K steps of c3 about
+// 2 us over a single CTA (14.3 against 12.3 us) with 16 to 64 CTAs, 4 us
+// with 152.
+constexpr int kMatchGrid = 32;
+
+int match_grid(int n_sm) {
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_match<false>, 1024, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_match<true>, 1024, 0) != cudaSuccess)
+    return 1;
+  const int per_sm = a < b ? a : b;
+  const int resident = per_sm > 0 ? per_sm * n_sm : 1;
+  return resident < kMatchGrid ? resident : kMatchGrid;
 }
 
 void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaStream_t s) {

@@ -69,7 +69,12 @@ struct LaunchShape {
   int block_stream;           // threads per block of those kernels
   int grid_pairs, block_pairs;
   int min_blocks;             // register-capped streaming kernels: 1 (none), 4 (64 regs), 6 (40 regs)
+  int grid_match;             // CTAs of the cooperative matcher (1 = one CTA, plain launch)
 };
+
+// CTAs of 1024 threads that the matcher can keep resident on n_sm SMs (the
+// size of its cooperative launch).
+int match_grid(int n_sm);
 
 // Called after each kernel of a step is enqueued (stage name); lets the
 // profiler record an event between kernels.  nullptr = no callback.
