@@ -141,6 +141,7 @@ _SIGS = {
     "bd_debug_get_slots": (C.c_int, [H, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_debug_get_cells": (C.c_int, [H, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_debug_withhold_scan": (C.c_int, [H, C.c_int]),
+    "bd_debug_withhold_match": (C.c_int, [H, C.c_int]),
     "bd_debug_get_pairs": (C.c_int, [H, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "bd_get_grid": (C.c_int, [H, C.c_int, P, P, P]),
     "bd_get_poisson_cdf": (C.c_int, [H, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_int),

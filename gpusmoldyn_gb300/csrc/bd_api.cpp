@@ -149,6 +149,7 @@ struct bd_system {
 
   bool host_only = false;  // BD_DEVICE_NONE: parameters and grid only
   bool scan_withhold = false;  // bd_debug_withhold_scan
+  bool match_withhold = false; // bd_debug_withhold_match
   std::vector<std::string> stage_names;  // kernels of one step (bd_profile_steps)
 
   // serving: instance slots filled and emptied while the handle runs
@@ -205,6 +206,7 @@ KParams make_params(bd_system* h) {
   p.tile_sums = h->tile_sums.p;
   p.scan_flags = h->scan_flags.p;
   p.scan_withhold = h->scan_withhold ? 1u : 0u;
+  p.match_withhold = h->match_withhold ? 1u : 0u;
   p.pairs = h->pairs.p;
   p.best = h->best.p;
   p.match_list = h->match_list.p;
@@ -1913,6 +1915,13 @@ BD_API bd_status bd_debug_get_slots(bd_handle h, float* xyz4, uint32_t* w, size_
 BD_API bd_status bd_debug_withhold_scan(bd_handle h, int on) {
   if (!h) return BD_ERR_INVALID_ARGUMENT;
   h->scan_withhold = on != 0;
+  if (h->graph1 || h->graphN) return build_graphs(h);
+  return BD_OK;
+}
+
+BD_API bd_status bd_debug_withhold_match(bd_handle h, int on) {
+  if (!h) return BD_ERR_INVALID_ARGUMENT;
+  h->match_withhold = on != 0;
   if (h->graph1 || h->graphN) return build_graphs(h);
   return BD_OK;
 }

@@ -1738,6 +1738,7 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
       c->match_next[0] = c->match_next[1] = 0;
       c->match_deaths = 0;
     }
+    if (p.match_withhold && blockIdx.x == 0) return;  // test switch: the other CTAs' waits run out
     if (!grid_barrier(c)) return;
     if (!match_rounds<true>(p, c, K, c->match_next)) return;
   } else {

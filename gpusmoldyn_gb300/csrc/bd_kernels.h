@@ -33,6 +33,7 @@ struct KParams {
   uint32_t* tile_sums;        // [n_tiles] scan partials
   unsigned long long* scan_flags; // [n_tiles] single-pass scan: state << 32 | sum, 0 between steps
   uint32_t scan_withhold;     // test switch: tile 0 of the scan does not publish (its successors time out)
+  uint32_t match_withhold;    // test switch: CTA 0 of the grid matcher never arrives (the others time out)
   DevPair* pairs;             // [pair_cap]
   unsigned long long* best;   // [capacity] matcher words, all ones between steps
   uint4* match_list;          // [2 * pair_cap] pending pairs (index, ends) of the matcher's rounds

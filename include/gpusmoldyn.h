@@ -255,6 +255,11 @@ BD_API bd_status bd_debug_get_cells(bd_handle h, uint32_t *start, size_t cap, si
  * for it runs out (after about a second) and the step reports
  * BD_ERR_TIMEOUT instead of hanging.  No fault, trap or endless loop. */
 BD_API bd_status bd_debug_withhold_scan(bd_handle h, int on);
+/* Test switch for the bounded waits of the matcher's grid barrier (steps
+ * with more than 8,192 candidate pairs): with on, CTA 0 of the matcher
+ * never arrives at its first barrier, so the other CTAs' waits run out
+ * (after about a second) and the step reports BD_ERR_TIMEOUT. */
+BD_API bd_status bd_debug_withhold_match(bd_handle h, int on);
 /* Candidate pairs (slot_i, slot_j, reaction, accepted) of the last step. */
 BD_API bd_status bd_debug_get_pairs(bd_handle h, uint32_t *quads, size_t cap, size_t *n);
 /* Uniform-grid geometry of one instance: cells per axis, cell edge lengths
