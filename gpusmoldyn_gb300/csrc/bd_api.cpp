@@ -366,7 +366,9 @@ bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int 
   h->shape.grid_stream = h->n_sm * 4;
   h->shape.min_blocks = 4;
   h->shape.block_pairs = 256;
-  h->shape.grid_pairs = h->n_sm * 8;
+  // one wave of the pair kernel (4 resident CTAs of 256 per SM): 0.2752
+  // against 0.2786 ms for two waves on the 16M c3 step
+  h->shape.grid_pairs = h->n_sm * 4;
   h->shape.grid_match = h->host_only ? 1 : match_grid(h->n_sm);
   memset(h->hctrl, 0, sizeof(DevCtrl));
   cudaMemset(h->ctrl.p, 0, sizeof(DevCtrl));

@@ -1033,14 +1033,11 @@ __device__ __forceinline__ uint32_t forward_key(uint32_t key0, uint32_t b, uint3
   return (uint32_t)((int)key0 + (dz * (int)d1 + dy) * (int)d0 + dx);
 }
 
-// Pairs of record r (canonical slot ca) with the records of neighbour cell
-// nkey, found from r's side.
+// Pairs of seeker k (canonical slot ca) with the records of neighbour cell
+// nkey (first slot ns, nn records), found from k's side.
 template <bool kBinned, bool kSingle>
-__device__ __forceinline__ void visit_neighbour(const KParams& p, DevCtrl* c, const float4& r, uint32_t ca,
-                                                uint32_t nkey, const float* s_maxr = nullptr, bool adv0 = true) {
-  Seeker k;
-  if (!seeker_init<kSingle>(p, r, k, s_maxr, adv0)) return;
-  const uint32_t ns = __ldg(&p.cell_start[nkey]), nn = __ldg(&p.cell_start[nkey + 1]) - ns;
+__device__ __forceinline__ void visit_cell(const KParams& p, DevCtrl* c, const Seeker& k, uint32_t ca,
+                                           uint32_t nkey, uint32_t ns, uint32_t nn) {
   if (nn > kBigCell) return;  // pairs with large cells are found by k_pairs_big_pairs
   const CellView nb = cell_records<kBinned>(p, nkey, ns);
   // x words of the first members together (overlapping latencies); a full
@@ -1126,7 +1123,8 @@ __device__ __forceinline__ void drain_faces(const KParams& p, DevCtrl* c, FaceQu
   while (nbm) {
     const uint32_t nkey = forward_key(key0, (uint32_t)(__ffs(nbm) - 1), I.dims[0], I.dims[1]);
     nbm &= nbm - 1u;
-    visit_neighbour<kBinned, kSingle>(p, c, r, ca, nkey, s_maxr, adv0);
+    const uint32_t ns = __ldg(&p.cell_start[nkey]);
+    visit_cell<kBinned, kSingle>(p, c, k, ca, nkey, ns, __ldg(&p.cell_start[nkey + 1]) - ns);
   }
 }
 

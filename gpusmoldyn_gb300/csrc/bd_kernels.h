@@ -95,7 +95,7 @@ void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaSt
 void enqueue_msd(const KParams& p, bool table, double* sum, unsigned long long* counts, cudaStream_t stream);
 
 // Tile size of the cell scan.
-constexpr uint32_t kScanTile = 16384;
+constexpr uint32_t kScanTile = 8192;
 
 // Places of a cell bin stored together (64 bytes); the bin capacity is a
 // multiple of it.

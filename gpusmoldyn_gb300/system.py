@@ -390,7 +390,7 @@ class System:
         L.check(self.lib.bd_instance_state(self.h, slot, C.byref(s), C.byref(f)), "bd_instance_state")
         return s.value, f.value
 
-    def set_launch_shape(self, block_stream=256, ctas_stream=4, block_pairs=256, ctas_pairs=8):
+    def set_launch_shape(self, block_stream=256, ctas_stream=4, block_pairs=256, ctas_pairs=4):
         L.check(self.lib.bd_set_launch_shape(self.h, block_stream, ctas_stream, block_pairs, ctas_pairs),
                 "bd_set_launch_shape")
 

@@ -31,7 +31,7 @@ def time_config(build, occupancy, shape, steps=20, warmup=5):
 
 
 def tune(build, occupancies=(1.5, 2.0, 3.0, 4.0, 6.0, 8.0),
-         shapes=((256, 4, 256, 8), (256, 8, 256, 8), (128, 8, 256, 8), (256, 4, 256, 4), (256, 4, 256, 16)),
+         shapes=((256, 4, 256, 4), (256, 8, 256, 4), (128, 8, 256, 4), (256, 4, 256, 8), (256, 4, 256, 16)),
          steps=20, warmup=5):
     """`build(occupancy)` returns a System with particles set.  Returns the
     best (occupancy, shape) and the timing table."""

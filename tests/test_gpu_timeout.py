@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def system(seed):
-    # 40^3 cells: several scan tiles of 16,384 cells, so a tile has a predecessor
+    # 40^3 cells: several scan tiles of 8,192 cells, so a tile has a predecessor
     s = System((0, 0, 0), (20, 20, 20), dt=1e-3, seed=seed, normals="table", cell_size=0.5)
     A, B = s.add_species(1.0), s.add_species(1.0)
     s.add_reaction(2, [A, B], [A], 1.0)
@@ -28,7 +28,7 @@ def system(seed):
 def test_scan_wait_runs_out_and_reports_timeout():
     s = system(71)
     dims, _, _ = s.grid()
-    assert int(np.prod(dims.astype(np.int64))) > 2 * 16384
+    assert int(np.prod(dims.astype(np.int64))) > 2 * 8192
     s.step(2)
     s.synchronize()
     L.check(s.lib.bd_debug_withhold_scan(s.h, 1), "withhold")
