@@ -126,6 +126,7 @@ struct bd_system {
   DevBuf<uint32_t> inst_step, inst_slot_base, zero_off;
   DevBuf<unsigned long long> events, pending;
   DevBuf<float4> state0, state1, scatter, bins;
+  cudaMemPool_t pool = nullptr;  // stream-ordered scratch of host transfers (keeps its memory)
   DevBuf<unsigned long long> best;
   DevBuf<uint32_t> cell_count, cell_start, tile_sums, big;
   DevBuf<uint4> match_list;
@@ -145,6 +146,9 @@ struct bd_system {
   float cell_override = 0.0f;
 
   cudaGraphExec_t graph1 = nullptr, graphN = nullptr;
+  KParams graph_params{};     // what the graphs in hand were captured with
+  LaunchShape graph_shape{};
+  Path graph_path = Path::kBinned;
   LaunchShape shape{};
 
   bool host_only = false;  // BD_DEVICE_NONE: parameters and grid only
@@ -241,10 +245,16 @@ KParams make_params(bd_system* h) {
 }
 
 bd_status build_graphs(bd_system* h) {
-  destroy_graphs(h);
   const KParams p = make_params(h);
   const bool table = h->cfg.normal_mode == BD_NORMALS_TABLE;
   const Path path = h->path();
+  // the graphs capture the parameter block, the launch shape and the path:
+  // when none of them changed (a new upload into the same buffers), the
+  // graphs in hand are still right
+  if (h->graph1 && h->graphN && path == h->graph_path && memcmp(&p, &h->graph_params, sizeof p) == 0 &&
+      memcmp(&h->shape, &h->graph_shape, sizeof h->shape) == 0)
+    return BD_OK;
+  destroy_graphs(h);
   const bool has_zero = h->Z > 0, has_uni = h->U > 0, has_bim = h->B > 0;
   for (int g = 0; g < 2; g++) {
     const int nsteps = g == 0 ? 1 : kGraphBatch;
@@ -258,6 +268,9 @@ bd_status build_graphs(bd_system* h) {
     BD_CUDA(e);
     (g == 0 ? h->graph1 : h->graphN) = exec;
   }
+  h->graph_params = p;
+  h->graph_shape = h->shape;
+  h->graph_path = path;
   return BD_OK;
 }
 
@@ -309,6 +322,21 @@ bd_status validate_config(const bd_config* c) {
   return BD_OK;
 }
 
+// The handle's pool for the scratch of host transfers, on its device; it
+// keeps the memory it maps until the handle is destroyed.
+cudaError_t create_pool(bd_system* h) {
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = h->device;
+  cudaError_t e = cudaMemPoolCreate(&h->pool, &props);
+  if (e != cudaSuccess) {
+    h->pool = nullptr;
+    return e;
+  }
+  uint64_t keep = UINT64_MAX;
+  return cudaMemPoolSetAttribute(h->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+}
 bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int n, bd_handle* out) {
   if (!out) return BD_ERR_INVALID_ARGUMENT;
   *out = nullptr;
@@ -354,6 +382,7 @@ bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int 
   }
   if (!cuda_ok(cudaSetDevice(h->device), "cudaSetDevice") ||
       !cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+      !cuda_ok(create_pool(h), "cudaMemPoolCreate") ||
       !cuda_ok(h->ctrl.alloc(1), "cudaMalloc ctrl") ||
       !cuda_ok(cudaMallocHost((void**)&h->hctrl, sizeof(DevCtrl)), "cudaMallocHost")) {
     bd_destroy(h);
@@ -529,6 +558,11 @@ bd_status layout_cells(bd_system* h) {
 
 // Device scratch of one call, taken from the stream-ordered pool and given
 // back on the stream when the call returns.
+// Stream-ordered scratch of one call (uploads, readbacks, admissions,
+// harvests), from the handle's own memory pool: the pool keeps the memory
+// it has mapped (release threshold: never), so a call that repeats a size
+// maps nothing new, where the device's default pool would hand the memory
+// back at each synchronisation and map it again on the next call.
 struct Scratch {
   cudaStream_t stream = nullptr;
   char* p = nullptr;
@@ -536,8 +570,9 @@ struct Scratch {
   ~Scratch() {
     if (p) cudaFreeAsync(p, stream);
   }
-  cudaError_t alloc(size_t bytes, cudaStream_t s) {
+  cudaError_t alloc(size_t bytes, cudaStream_t s, cudaMemPool_t pool) {
     stream = s;
+    if (pool) return cudaMallocFromPoolAsync((void**)&p, bytes, pool, s);
     return cudaMallocAsync((void**)&p, bytes, s);
   }
   template <class T>
@@ -592,7 +627,7 @@ bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, 
     BD_CUDA(cudaSetDevice(h->device));
     BD_CUDA(scratch.alloc(scratch_bytes({n * sizeof(float4), n * sizeof(int), (I + 1) * sizeof(uint64_t),
                                          boxes.size() * sizeof(float), sizeof(uint32_t)}),
-                          h->stream));
+                          h->stream, h->pool));
     float4* d_xyz4 = scratch.take<float4>(n);
     int* d_species = scratch.take<int>(n);
     uint64_t* d_start = scratch.take<uint64_t>(I + 1);
@@ -729,6 +764,7 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->dpbox_list.free();
   h->surf_queue.free();
   h->dcell_surf.free();
+  if (h->pool) cudaMemPoolDestroy(h->pool);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return BD_OK;
@@ -1380,7 +1416,7 @@ BD_API bd_status bd_get_instance_particles(bd_handle h, int inst, float* xyz4, i
   Scratch scratch;
   BD_CUDA(scratch.alloc(scratch_bytes({slots * sizeof(float4), slots * sizeof(int), tiles * sizeof(uint32_t),
                                        sizeof(uint32_t)}),
-                        h->stream));
+                        h->stream, h->pool));
   ExportArgs a{};
   a.state = h->hctrl->cur ? h->state1.p : h->state0.p;
   a.n_slots = slots;
@@ -1545,7 +1581,7 @@ BD_API bd_status bd_instance_admit(bd_handle h, const bd_instance_desc* d, const
     const float box[6] = {dd.box_lo[0], dd.box_lo[1], dd.box_lo[2], dd.box_hi[0], dd.box_hi[1], dd.box_hi[2]};
     BD_CUDA(scratch.alloc(scratch_bytes({n * sizeof(float4), n * sizeof(int), sizeof(start), sizeof(box),
                                          sizeof(uint32_t)}),
-                          h->stream));
+                          h->stream, h->pool));
     float4* d_xyz4 = scratch.take<float4>(n);
     int* d_species = scratch.take<int>(n);
     uint64_t* d_start = scratch.take<uint64_t>(2);
@@ -1683,7 +1719,7 @@ BD_API bd_status bd_instance_harvest(bd_handle h, int k, float* xyz4, int* speci
     Scratch scratch;
     BD_CUDA(scratch.alloc(scratch_bytes({len * sizeof(float4), len * sizeof(int), tiles * sizeof(uint32_t),
                                          sizeof(uint32_t)}),
-                          h->stream));
+                          h->stream, h->pool));
     ExportArgs a{};
     a.state = cur + base[k];
     a.n_slots = len;
