@@ -1061,10 +1061,17 @@ __device__ __forceinline__ void visit_cell(const KParams& p, DevCtrl* c, const S
   }
 }
 
-// Canonical order + pair search, one warp per 32 consecutive cells.  The
-// warp walks the cells' records 32 at a time (lane t of a round = record t
-// of the cells' concatenation), so each lane handles one record whatever
-// the cell sizes; there are no CTA-wide barriers.  For its record a lane
+// Canonical order + pair search.  A warp takes tasks of 32 consecutive
+// cells, from the highest key down, and strings the tasks' records
+// together into one stream: round r of the warp takes stream records
+// 32r .. 32r+31, one per lane, whatever cells and tasks they come from, so
+// only the warp's last round runs partly empty.  (Rounds that stopped at
+// each task's end left 14% of the lanes idle on the 16M c3 step, whose
+// tasks hold about 97 records.)  At most two tasks are open at a time:
+// their non-empty cells sit in a per-warp ring, and a task is opened (its
+// cell ranges read and scanned) when the stream runs short of the next
+// round and the task before the last one has ended.  There are no CTA-wide
+// barriers.  For its record a lane
 //   * counts the records of its cell that precede it in canonical order,
 //     reading only their x words (records whose x bits occur twice in the
 //     cell are ranked again on all four words), and writes it to
@@ -1091,6 +1098,7 @@ __device__ __forceinline__ void visit_cell(const KParams& p, DevCtrl* c, const S
 constexpr bool kStagePairs = false;
 
 constexpr uint32_t kFaceQueue = 64;  // queued records per warp (< 32 between drains, + one round's push)
+constexpr uint32_t kCellRing = 64;   // open cells per warp: two tasks of at most 32 non-empty cells
 
 // Records near a +face queued by a warp.
 struct FaceQueue {
@@ -1130,17 +1138,18 @@ __device__ __forceinline__ void drain_faces(const KParams& p, DevCtrl* c, FaceQu
 
 // kStage (binned path): group 0 of a task's 32 cells -- their first
 // kBinGroup places, one contiguous 2 KiB run of the bins -- is brought into
-// shared memory by a bulk copy, double-buffered per warp: the copy for the
-// warp's next task is started before the current task's rounds, so the
-// copy engine moves it while the warp works and the rounds read the first
-// places of every cell (most cells hold at most kBinGroup records) from
-// shared memory.  Places beyond the first group are read from global
-// memory.
+// shared memory by a bulk copy into the stage buffer of the task's slot
+// (its index among the warp's tasks, mod 2).  The copy for a task is
+// started as soon as the task two before it has ended, so the copy engine
+// moves it while the warp works on the task in between; it is waited for
+// when the task is opened.  Places beyond the first group are read from
+// global memory.
 template <bool kHasBim, bool kBinned, bool kSingle, bool kStage>
 __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
-  // per non-empty cell of the task: (key, first slot) and (records | offset << 8)
-  __shared__ uint2 s_cell[8][32];
-  __shared__ uint32_t s_noff[8][32];
+  // ring of the open tasks' non-empty cells: (key, first slot) and
+  // (records | task slot << 8, stream offset of the cell's first record)
+  __shared__ uint2 s_cell[8][kCellRing];
+  __shared__ uint2 s_meta[8][kCellRing];
   __shared__ FaceQueue s_face[kHasBim ? 8 : 1];
   __shared__ float s_maxr[kSingle ? kCtxSpecies : 1];
   __shared__ __align__(128) float4 s_stage[kStage ? 8 : 1][kStage ? 2 : 1][kStage ? 32 * kBinGroup : 1];
@@ -1157,150 +1166,185 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
   const uint32_t n_tasks = (p.n_cells + 31u) >> 5;
   const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  const uint32_t tk0 = blockIdx.x * (blockDim.x >> 5) + warp;
+  const uint32_t my_tasks = tk0 < n_tasks ? (n_tasks - 1u - tk0) / nw + 1u : 0u;
   const uint32_t le_mask = lane == 31 ? kFull : ((2u << lane) - 1u);
   FaceQueue& fqueue = s_face[kHasBim ? warp : 0];
   uint32_t fq = 0;  // queued records (warp-uniform)
-  const uint32_t tk0 = blockIdx.x * (blockDim.x >> 5) + warp;
-  // group 0 of task `task` into stage buffer b (lane 0)
-  auto stage = [&](uint32_t task, uint32_t b) {
-    const uint32_t first = task * 32u, cells = min(32u, p.n_cells - first);
-    bulk_to_smem(&s_stage[kStage ? warp : 0][kStage ? b : 0][0], p.bins + bin_index(p, first, 0),
-                 cells * kBinGroup * (uint32_t)sizeof(float4), &s_bar[kStage ? warp : 0][b]);
+  // The warp's i-th task.  Cells are taken from the highest key down: the
+  // bins written last by k_bin (its records stream in ascending cell
+  // order) are still in L2, and the next state's low slots, written last
+  // here, are the first the next step's k_bin reads.
+  auto task_of = [&](uint32_t i) { return n_tasks - 1u - (tk0 + i * nw); };
+  // group 0 of the i-th task's cells into stage buffer i & 1 (lane 0)
+  auto stage = [&](uint32_t i) {
+    const uint32_t first = task_of(i) * 32u, cells = min(32u, p.n_cells - first);
+    bulk_to_smem(&s_stage[kStage ? warp : 0][kStage ? (i & 1u) : 0][0], p.bins + bin_index(p, first, 0),
+                 cells * kBinGroup * (uint32_t)sizeof(float4), &s_bar[kStage ? warp : 0][kStage ? (i & 1u) : 0]);
   };
-  uint32_t phase = 0;  // bit b: parity of stage buffer b's next completion
+  uint32_t staged = 0;  // tasks whose copies have been started
   if (kStage) {
+    staged = min(my_tasks, 2u);
     if (lane == 0) {
       mbar_init(&s_bar[warp][0]);
       mbar_init(&s_bar[warp][1]);
       mbar_init_fence();
-      if (tk0 < n_tasks) stage(n_tasks - 1u - tk0, 0);
+      for (uint32_t i = 0; i < staged; ++i) stage(i);
     }
     __syncwarp();
   }
-  // Cells are taken from the highest key down: the bins written last by
-  // k_bin (its records stream in ascending cell order) are still in L2,
-  // and the next state's low slots, written last here, are the first the
-  // next step's k_bin reads.
-  uint32_t it = 0;
-  for (uint32_t tk = tk0; tk < n_tasks; tk += nw, ++it) {
-    const uint32_t task = n_tasks - 1u - tk;
-    const uint32_t cell = task * 32u + lane;
-    const uint32_t buf = it & 1u;
-    if (kStage && lane == 0 && tk + nw < n_tasks) stage(n_tasks - 1u - (tk + nw), buf ^ 1u);
-    uint32_t cs = 0, n = 0;
-    if (cell < p.n_cells) {
-      cs = __ldg(&p.cell_start[cell]);
-      n = __ldg(&p.cell_start[cell + 1]) - cs;
-      if (kBinned) p.cell_count[cell] = 0u;
-      if (n > kBigCell) {
-        const uint32_t b = atomicAdd(&c->n_big, 1u);
-        if (b < p.big_cap) p.big[b] = cell;
-        else atomicOr(&c->status, kStatBounds);
-        n = 0;
+  // The two task slots (slot = task index & 1): the stream offset of the
+  // lane's cell in each, ~0 for an empty cell.
+  uint32_t o0 = ~0u, o1 = ~0u;
+  uint32_t opened = 0;   // tasks opened
+  uint32_t last = 0;     // stream offset of the last opened task (the end of the one before it)
+  uint32_t loaded = 0;   // stream records of the opened tasks
+  uint32_t entries = 0;  // ring entries written
+  uint32_t before = 0;   // ring entries whose cells start before the round
+  // A round takes stream records [rb, rb + 32); one that the open tasks
+  // cannot fill (the last task before it still open, or no task left)
+  // ends at `loaded`, where the next round starts.
+  for (uint32_t rb = 0;;) {
+    // Open tasks while the stream falls short of this round and the slot
+    // to be reused holds a task that has ended.
+    while (loaded < rb + 32u && opened < my_tasks && last <= rb) {
+      const uint32_t sl = opened & 1u;
+      if (kStage && staged == opened) {  // its copy was not started early
+        if (lane == 0) stage(opened);
+        ++staged;
       }
-    }
-    const uint32_t q = __popc(__ballot_sync(kFull, n > 0) & ((1u << lane) - 1u));
-    uint32_t incl = n;
+      const uint32_t cell = task_of(opened) * 32u + lane;
+      uint32_t cs = 0, n = 0;
+      if (cell < p.n_cells) {
+        cs = __ldg(&p.cell_start[cell]);
+        n = __ldg(&p.cell_start[cell + 1]) - cs;
+        if (kBinned) p.cell_count[cell] = 0u;
+        if (n > kBigCell) {
+          const uint32_t b = atomicAdd(&c->n_big, 1u);
+          if (b < p.big_cap) p.big[b] = cell;
+          else atomicOr(&c->status, kStatBounds);
+          n = 0;
+        }
+      }
+      const uint32_t ball = __ballot_sync(kFull, n > 0);
+      uint32_t incl = n;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t t = __shfl_up_sync(kFull, incl, d);
-      if (lane >= (uint32_t)d) incl += t;
-    }
-    const uint32_t off = incl - n, total = __shfl_sync(kFull, incl, 31);
-    if (n > 0) {
-      s_cell[warp][q] = make_uint2(cell, cs);
-      s_noff[warp][q] = n | (off << 8);
-    }
-    __syncwarp();
-    if (kStage) {
-      if (!mbar_wait(&s_bar[warp][buf], (phase >> buf) & 1u)) {
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, d);
+        if (lane >= (uint32_t)d) incl += t;
+      }
+      const uint32_t off = loaded + incl - n;
+      __syncwarp();  // the ring entries about to be replaced are no longer read
+      if (n > 0) {
+        const uint32_t e = (entries + __popc(ball & ((1u << lane) - 1u))) & (kCellRing - 1u);
+        s_cell[warp][e] = make_uint2(cell, cs);
+        s_meta[warp][e] = make_uint2(n | (sl << 8), off);
+      }
+      entries += __popc(ball);
+      last = loaded;
+      loaded += __shfl_sync(kFull, incl, 31);
+      if (sl) o1 = n > 0 ? off : ~0u;
+      else o0 = n > 0 ? off : ~0u;
+      if (kStage && !mbar_wait(&s_bar[warp][sl], (opened >> 1) & 1u)) {
+        // give up: record the timeout and let the copies still in flight land
         if (lane == 0) atomicOr(&c->status, kStatTimeout);
+        for (uint32_t i = opened; i < staged; ++i) mbar_wait(&s_bar[warp][i & 1u], (i >> 1) & 1u);
         return;
       }
-      phase ^= 1u << buf;
+      ++opened;
+      __syncwarp();
     }
-    const float4* stage_base = &s_stage[kStage ? warp : 0][kStage ? buf : 0][0];
-    uint32_t before = 0;  // non-empty cells that start before this round
-    for (uint32_t rb = 0; rb < total; rb += 32u) {
-      const uint32_t M = __reduce_or_sync(kFull, (n > 0 && off >= rb && off - rb < 32u) ? 1u << (off - rb) : 0u);
-      const uint32_t t = rb + lane;
-      bool near = false;  // this lane's record may have partners in forward neighbour cells
-      uint32_t ca = 0;
-      float4 ra = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (t < total) {
-        const uint32_t oq = before + __popc(M & le_mask) - 1u;
-        const uint2 cc = s_cell[warp][oq];
-        const uint32_t no = s_noff[warp][oq];
-        const uint32_t ocell = cc.x, ocs = cc.y, on = no & 0xFFu;
-        const uint32_t j = t - (no >> 8);
-        const BinView<kStage> cb{stage_base + (ocell - task * 32u) * kBinGroup, cell_records<kBinned>(p, ocell, ocs)};
-        ra = cb.ldg(j);
-        Seeker k;
-        const bool search = kHasBim && seeker_init<kSingle>(p, ra, k, kSingle ? s_maxr : nullptr, adv0);
-        const float xlim = search ? k.xlim : -1.0f;
-        const uint32_t rx = __float_as_uint(ra.x);
-        // rank: members with smaller x bits; le also counts equal ones (the
-        // record itself among them), so le - rank > 1 means a tie to break
-        // on all four words.  cand: bit m = member m < 32 with |dx| in range
-        // The first kRankBatch x words are loaded together, so their
-        // latencies overlap (each group of kBinGroup members lies on its
-        // own line); larger cells continue one member at a time.
-        constexpr uint32_t kRankBatch = 8;
-        uint32_t rank = 0, le = 0, cand = 0;
-        float xs[kRankBatch];
+    if (rb >= loaded) break;  // every task opened and taken
+    // lanes at which a cell starts in this round
+    const uint32_t M = __reduce_or_sync(kFull, (o0 - rb < 32u ? 1u << (o0 - rb) : 0u) |
+                                                   (o1 - rb < 32u ? 1u << (o1 - rb) : 0u));
+    const uint32_t t = rb + lane;
+    bool near = false;  // this lane's record may have partners in forward neighbour cells
+    uint32_t ca = 0;
+    float4 ra = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (t < loaded) {
+      const uint32_t e = (before + __popc(M & le_mask) - 1u) & (kCellRing - 1u);
+      const uint2 cc = s_cell[warp][e];
+      const uint2 meta = s_meta[warp][e];
+      const uint32_t ocell = cc.x, ocs = cc.y, on = meta.x & 0xFFu;
+      const uint32_t j = t - meta.y;
+      const BinView<kStage> cb{&s_stage[kStage ? warp : 0][kStage ? (meta.x >> 8) : 0][kStage ? (ocell & 31u) * kBinGroup : 0],
+                               cell_records<kBinned>(p, ocell, ocs)};
+      ra = cb.ldg(j);
+      Seeker k;
+      const bool search = kHasBim && seeker_init<kSingle>(p, ra, k, kSingle ? s_maxr : nullptr, adv0);
+      const float xlim = search ? k.xlim : -1.0f;
+      const uint32_t rx = __float_as_uint(ra.x);
+      // rank: members with smaller x bits; le also counts equal ones (the
+      // record itself among them), so le - rank > 1 means a tie to break
+      // on all four words.  cand: bit m = member m < 32 with |dx| in range
+      // The first kRankBatch x words are loaded together, so their
+      // latencies overlap (each group of kBinGroup members lies on its
+      // own line); larger cells continue one member at a time.
+      constexpr uint32_t kRankBatch = 8;
+      uint32_t rank = 0, le = 0, cand = 0;
+      float xs[kRankBatch];
 #pragma unroll
-        for (uint32_t m = 0; m < kRankBatch; ++m) xs[m] = m < on ? cb.ldg_x(m) : 0.0f;
+      for (uint32_t m = 0; m < kRankBatch; ++m) xs[m] = m < on ? cb.ldg_x(m) : 0.0f;
 #pragma unroll
-        for (uint32_t m = 0; m < kRankBatch; ++m) {
-          if (m >= on) break;
-          const uint32_t qb = __float_as_uint(xs[m]);
-          rank += qb < rx ? 1u : 0u;
-          le += qb <= rx ? 1u : 0u;
-          if (fabsf(__fsub_rn(xs[m], ra.x)) <= xlim) cand |= 1u << m;
-        }
-        for (uint32_t m = kRankBatch; m < on; ++m) {
-          const float qx = cb.ldg_x(m);
-          const uint32_t qb = __float_as_uint(qx);
-          rank += qb < rx ? 1u : 0u;
-          le += qb <= rx ? 1u : 0u;
-          if (m < 32u && fabsf(__fsub_rn(qx, ra.x)) <= xlim) cand |= 1u << m;
-        }
-        cand &= j >= 31u ? 0u : ~((2u << j) - 1u);  // later members only
-        if (le - rank > 1u) rank = canonical_rank(cb, 0, on, j, ra);
-        ca = ocs + rank;
-        if (ca < p.capacity) nx[ca] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
-        else atomicOr(&c->status, kStatBounds);
-        if (search) {
-          while (cand) {
-            const uint32_t m = (uint32_t)(__ffs(cand) - 1);
-            cand &= cand - 1u;
-            const float4 qm = cb.ldg(m);
-            const int32_t bb = pair_reaction(p, k, qm);
-            if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
-          }
-          for (uint32_t m = max(j + 1u, 32u); m < on; ++m) {  // cells of 33..kBigCell records
-            const float4 qm = cb.ldg(m);
-            const int32_t bb = pair_reaction(p, k, qm);
-            if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
-          }
-          near = near_forward_face<kSingle>(p, k);
-        }
+      for (uint32_t m = 0; m < kRankBatch; ++m) {
+        if (m >= on) break;
+        const uint32_t qb = __float_as_uint(xs[m]);
+        rank += qb < rx ? 1u : 0u;
+        le += qb <= rx ? 1u : 0u;
+        if (fabsf(__fsub_rn(xs[m], ra.x)) <= xlim) cand |= 1u << m;
       }
-      if (kHasBim) {
-        // records near a +face into the warp's queue, visited 32 at a time
-        const uint32_t ball = __ballot_sync(kFull, near);
-        if (near) {
-          const uint32_t pos = fq + __popc(ball & ((1u << lane) - 1u));
-          fqueue.rec[pos] = ra;
-          fqueue.ca[pos] = ca;
-        }
-        fq += __popc(ball);
-        if (fq >= 32u) {
-          drain_faces<kBinned, kSingle>(p, c, fqueue, fq, kSingle ? s_maxr : nullptr, adv0);
-          fq -= 32u;
-        }
+      for (uint32_t m = kRankBatch; m < on; ++m) {
+        const float qx = cb.ldg_x(m);
+        const uint32_t qb = __float_as_uint(qx);
+        rank += qb < rx ? 1u : 0u;
+        le += qb <= rx ? 1u : 0u;
+        if (m < 32u && fabsf(__fsub_rn(qx, ra.x)) <= xlim) cand |= 1u << m;
       }
-      before += __popc(M);
+      cand &= j >= 31u ? 0u : ~((2u << j) - 1u);  // later members only
+      if (le - rank > 1u) rank = canonical_rank(cb, 0, on, j, ra);
+      ca = ocs + rank;
+      if (ca < p.capacity) nx[ca] = make_float4(ra.x, ra.y, ra.z, __uint_as_float(rec_w(ra) & ~kNewborn));
+      else atomicOr(&c->status, kStatBounds);
+      if (search) {
+        while (cand) {
+          const uint32_t m = (uint32_t)(__ffs(cand) - 1);
+          cand &= cand - 1u;
+          const float4 qm = cb.ldg(m);
+          const int32_t bb = pair_reaction(p, k, qm);
+          if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
+        }
+        for (uint32_t m = max(j + 1u, 32u); m < on; ++m) {  // cells of 33..kBigCell records
+          const float4 qm = cb.ldg(m);
+          const int32_t bb = pair_reaction(p, k, qm);
+          if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
+        }
+        near = near_forward_face<kSingle>(p, k);
+      }
+    }
+    if (kHasBim) {
+      // records near a +face into the warp's queue, visited 32 at a time
+      const uint32_t ball = __ballot_sync(kFull, near);
+      if (near) {
+        const uint32_t pos = fq + __popc(ball & ((1u << lane) - 1u));
+        fqueue.rec[pos] = ra;
+        fqueue.ca[pos] = ca;
+      }
+      fq += __popc(ball);
+      if (fq >= 32u) {
+        drain_faces<kBinned, kSingle>(p, c, fqueue, fq, kSingle ? s_maxr : nullptr, adv0);
+        fq -= 32u;
+      }
+    }
+    before += __popc(M);
+    rb = min(rb + 32u, loaded);
+    // kStage: once the task two before the next unstaged one (the last
+    // opened task, or the one before it) has ended with this round, its
+    // buffer takes that task's copy
+    if (kStage && staged < my_tasks && staged <= opened + 1u && (staged > opened ? loaded : last) <= rb) {
+      __syncwarp();
+      if (lane == 0) stage(staged);
+      ++staged;
     }
     __syncwarp();
   }

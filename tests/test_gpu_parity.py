@@ -327,6 +327,31 @@ def test_clusters_across_cell_corners_bit_exact(sort):
     assert npairs > 0 and ev[0] > 0
 
 
+@pytest.mark.parametrize("sort", SORTS)
+def test_sparse_clumps_bit_exact(sort):
+    """About a million small cells, most of them empty, with the particles in
+    small clumps: the pair kernel's warps string many tasks (32 cells each)
+    into one record stream, most tasks empty and the rest holding a few
+    records, so rounds that the open tasks cannot fill, tasks opened after
+    such a round and empty tasks between full ones all occur.  A record
+    skipped or taken twice changes the slots and the pairs."""
+    side, n_clumps, per = 20.0, 3000, 24
+    s = System((0, 0, 0), (side,) * 3, dt=1e-3, seed=41, normals="table", sort=sort, cell_size=0.2)
+    A, B, Cc = s.add_species(0.05), s.add_species(0.05), s.add_species(0.02)
+    s.add_reaction(2, [A, B], [Cc], 0.2)
+    s.finalize()
+    g = rng(41)
+    centres = uniform_positions(g, n_clumps, (0.2, 0.2, 0.2), (side - 0.2,) * 3)
+    pos = np.repeat(centres, per, axis=0) + (g.random((n_clumps * per, 3), dtype=np.float32) - 0.5) * 0.3
+    pos = np.clip(pos, 0.0, side).astype(np.float32)
+    sp = (np.arange(len(pos)) % 2).astype(np.int32)
+    s.set_particles(pos, sp)
+    dims, _, _ = s.grid()
+    assert int(np.prod(dims.astype(np.int64))) >= 900_000
+    _, npairs, ev = run_parity(s, 3)
+    assert npairs > 100 and ev[0] > 0
+
+
 def test_steps_ordered_on_a_caller_stream():
     """bd_step_async on another stream gives the same trajectory as bd_step."""
     torch = pytest.importorskip("torch")
