@@ -130,7 +130,6 @@ struct bd_system {
   DevBuf<unsigned long long> best;
   DevBuf<uint32_t> cell_count, cell_start, tile_sums, big;
   DevBuf<uint4> match_list;
-  DevBuf<unsigned long long> scan_flags;
   DevBuf<float4> big_scratch;  // allocated when a cell first outgrows the pair kernel
   DevBuf<DevPair> pairs;
 
@@ -208,7 +207,6 @@ KParams make_params(bd_system* h) {
   p.cell_count = h->cell_count.p;
   p.cell_start = h->cell_start.p;
   p.tile_sums = h->tile_sums.p;
-  p.scan_flags = h->scan_flags.p;
   p.scan_withhold = h->scan_withhold ? 1u : 0u;
   p.match_withhold = h->match_withhold ? 1u : 0u;
   p.pairs = h->pairs.p;
@@ -399,6 +397,7 @@ bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int 
   // against 0.2786 ms for two waves on the 16M c3 step
   h->shape.grid_pairs = h->n_sm * 4;
   h->shape.grid_match = h->host_only ? 1 : match_grid(h->n_sm);
+  h->shape.grid_scan = h->host_only ? 1 : scan_grid(h->n_sm);
   memset(h->hctrl, 0, sizeof(DevCtrl));
   cudaMemset(h->ctrl.p, 0, sizeof(DevCtrl));
   *out = h;
@@ -531,8 +530,6 @@ bd_status layout_cells(bd_system* h) {
   BD_CUDA(ensure(h->cell_start, (size_t)h->n_cells + 1));
   BD_CUDA(cudaMemsetAsync(h->cell_start.p, 0, ((size_t)h->n_cells + 1) * sizeof(uint32_t), h->stream));
   BD_CUDA(ensure(h->tile_sums, (size_t)std::max<uint32_t>(h->n_tiles, 1)));
-  BD_CUDA(ensure(h->scan_flags, (size_t)std::max<uint32_t>(h->n_tiles, 1)));
-  BD_CUDA(cudaMemsetAsync(h->scan_flags.p, 0, h->scan_flags.n * sizeof(unsigned long long), h->stream));
   BD_CUDA(cudaStreamSynchronize(h->stream));
   if (!h->panels.empty()) {
     const bd_status st = upload_cell_masks(h);
@@ -755,7 +752,6 @@ BD_API bd_status bd_destroy(bd_handle h) {
   h->cell_count.free();
   h->cell_start.free();
   h->tile_sums.free();
-  h->scan_flags.free();
   h->pairs.free();
   h->match_list.free();
   h->dpanels.free();
@@ -1339,12 +1335,10 @@ BD_API bd_status bd_synchronize(bd_handle h) {
       }
       BD_CUDA(cudaMemsetAsync(h->cell_count.p, 0, (size_t)h->n_cells * sizeof(uint32_t), h->stream));
       BD_CUDA(cudaMemsetAsync(h->pending.p, 0, h->pending.n * sizeof(unsigned long long), h->stream));
-      BD_CUDA(cudaMemsetAsync(h->scan_flags.p, 0, h->scan_flags.n * sizeof(unsigned long long), h->stream));
       c.status = 0;
       c.n_pairs = 0;
       c.n_big = 0;
       c.n_surf = 0;
-      c.scan_ticket = 0;
       c.surf_ticket = 0;
       c.n_virtual = 0;
       c.bar_count = 0;

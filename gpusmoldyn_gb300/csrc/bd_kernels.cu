@@ -462,119 +462,39 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_count(KParams p) {
   });
 }
 
-// Single-pass exclusive scan of the cell counts into cell_start, by
-// decoupled look-back (D. Merrill
-// and M. Garland, "Single-pass parallel prefix scan with decoupled
-// look-back", NVIDIA NVR-2016-002).  Each CTA takes the next tile by an
-// atomic ticket, so a tile only ever waits on tiles that CTAs already
-// running have taken; it publishes its sum (kScanAggregate), adds the
-// sums published before it, walking back until a tile that knows its full
-// prefix (kScanInclusive), and publishes that.  The first warp does the
-// walk, 32 predecessors per poll, with at most kScanPolls polls that find a
-// flag not yet written, after which the step stops with kStatTimeout.  The flags and the ticket are cleared when
-// the step commits (k_match) and by the host before a replay.
-constexpr unsigned long long kScanAggregate = 1ull << 32, kScanInclusive = 2ull << 32;
-constexpr uint32_t kScanPolls = 1u << 20;
+// Grid-wide barrier of a cooperative launch (every CTA resident): thread 0
+// of each CTA reads the generation, arrives on the counter, and either (the
+// last to arrive) resets the counter and advances the generation, or waits
+// for the generation to change.  The wait is bounded: after kGridSpins polls
+// the CTA raises kStatTimeout and the barrier returns false; the other CTAs
+// then run out at the same barrier or the next, so every CTA returns.
+constexpr uint32_t kGridSpins = 1u << 22;
 
-__device__ __forceinline__ void store_release(unsigned long long* a, unsigned long long v) {
-  asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long load_acquire(const unsigned long long* a) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
-  return v;
-}
-
-__global__ void __launch_bounds__(1024) k_scan(KParams p) {
-  __shared__ uint32_t s_tile, s_total, s_prefix, s_stop;
-  DevCtrl* c = p.ctrl;
-  if (threadIdx.x == 0) {
-    s_stop = ld_u32(&c->status) != 0u;
-    if (!s_stop) s_tile = atomicAdd(&c->scan_ticket, 1u);
-  }
+__device__ bool grid_barrier(DevCtrl* c) {
+  __shared__ uint32_t s_ok;
   __syncthreads();
-  if (s_stop || s_tile >= p.n_tiles) return;  // uniform over the CTA
-  const uint32_t tile = s_tile;
-  constexpr uint32_t kPer = kScanTile / 1024;  // consecutive counts per thread, 16-byte aligned
-  static_assert(kPer % 4 == 0, "vector loads of 4 counts");
-  const uint32_t base = tile * kScanTile + threadIdx.x * kPer;
-  const bool whole = base + kPer <= p.n_cells;
-  uint32_t v[kPer];
-  uint32_t sum = 0;
-#pragma unroll
-  for (uint32_t k = 0; k < kPer; k += 4) {
-    if (whole) {
-      const uint4 q = __ldcg(reinterpret_cast<const uint4*>(p.cell_count + base + k));
-      v[k] = q.x, v[k + 1] = q.y, v[k + 2] = q.z, v[k + 3] = q.w;
+  if (threadIdx.x == 0) {
+    s_ok = 1u;
+    const uint32_t gen = *(volatile uint32_t*)&c->bar_gen;
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1u) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
     } else {
-#pragma unroll
-      for (uint32_t e = 0; e < 4; ++e) v[k + e] = base + k + e < p.n_cells ? ld_u32(&p.cell_count[base + k + e]) : 0u;
-    }
-  }
-#pragma unroll
-  for (uint32_t k = 0; k < kPer; ++k) sum += v[k];
-  const uint32_t excl = block_exclusive_scan<1024>(sum, &s_total);
-  if (threadIdx.x < 32) {
-    // the look-back, one warp: lane l reads the flag of tile pred - l, so a
-    // poll resolves up to 32 predecessors
-    const uint32_t lane = threadIdx.x, agg = s_total;
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      if (lane == 0) store_release(&p.scan_flags[tile], kScanAggregate | agg);
-      int32_t pred = (int32_t)tile - 1;
-      uint32_t polls = 0;
-      for (;;) {
-        const int32_t t = pred - (int32_t)lane;
-        // before tile 0 there is nothing: an inclusive sum of 0
-        const unsigned long long f = t >= 0 ? load_acquire(&p.scan_flags[t]) : kScanInclusive;
-        const uint32_t inc = __ballot_sync(kFull, (f & kScanInclusive) != 0ull);
-        const uint32_t ready = __ballot_sync(kFull, f != 0ull);
-        const uint32_t upto = inc ? (uint32_t)(__ffs(inc) - 1) : 31u;  // nearest inclusive flag
-        const uint32_t need = upto == 31u ? kFull : ((2u << upto) - 1u);
-        if ((ready & need) == need) {
-          uint32_t v = lane <= upto ? (uint32_t)f : 0u;
-#pragma unroll
-          for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
-          prefix += v;
-          if (inc) break;
-          pred -= 32;
-          continue;
-        }
-        if (++polls > kScanPolls) {
-          if (lane == 0) atomicOr(&c->status, kStatTimeout);
+      for (uint32_t spins = 0; *(volatile uint32_t*)&c->bar_gen == gen; ++spins) {
+        if (spins > kGridSpins) {
+          atomicOr(&c->status, kStatTimeout);
+          s_ok = 0u;
           break;
         }
+        __nanosleep(64);
       }
     }
-    if (lane == 0) {
-      if (!(p.scan_withhold && tile == 0)) store_release(&p.scan_flags[tile], kScanInclusive | (prefix + agg));
-      s_prefix = prefix;
-      if (tile == p.n_tiles - 1) {
-        const uint32_t total = prefix + agg;
-        p.cell_start[p.n_cells] = total;
-        c->n_sorted = total;
-        if (total > p.capacity) atomicOr(&c->status, kStatCapacity);
-      }
-    }
+    __threadfence();
   }
   __syncthreads();
-  uint32_t run = s_prefix + excl;
-#pragma unroll
-  for (uint32_t k = 0; k < kPer; ++k) {
-    const uint32_t x = v[k];
-    v[k] = run;
-    run += x;
-  }
-#pragma unroll
-  for (uint32_t k = 0; k < kPer; k += 4) {
-    if (whole) {
-      *reinterpret_cast<uint4*>(p.cell_start + base + k) = make_uint4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-    } else {
-#pragma unroll
-      for (uint32_t e = 0; e < 4; ++e)
-        if (base + k + e < p.n_cells) p.cell_start[base + k + e] = v[k + e];
-    }
-  }
+  return s_ok != 0u;
 }
 
 template <bool kTable, int kMinBlocks, bool kSingle, int kSurf = 0>
@@ -846,6 +766,143 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (done) return true;
   }
   return false;
+}
+
+// Exclusive scan of the cell counts into cell_start, by a cooperative grid
+// of two CTAs per SM (every CTA resident).  CTA b owns a contiguous range of
+// cells and moves it through shared memory in chunks of up to kScanChunk
+// counts, each brought in by one bulk copy (the copy engine, not a load
+// per word): pass 1 sums the range and publishes the sum (tile_sums[b]);
+// after one grid barrier, pass 2 adds the sums of the CTAs before it,
+// scans each chunk in shared memory (a contiguous run of counts per
+// thread) and writes it out by one bulk copy.  On the 16M c3 step a range
+// is one chunk, so pass 2 finds it still in shared memory.  The last 1..3
+// counts of the grid that do not fill 16 bytes go by plain loads and
+// stores.  20.8 us on the 16M c3 step; chunks of 49,152 counts (one CTA
+// per SM) took 22.4 us, of 12,288 (four) 26.3 us.  Earlier forms: a
+// single-pass scan by decoupled look-back, 27 us (643 tiles, and the
+// frontier of known prefixes moved by the 32 flags one poll reads per round
+// trip); this grid scan reading tiles of 8,192 counts with vector loads
+// instead of staging them, 24.6 us.
+constexpr uint32_t kScanChunk = 24576;  // counts per chunk: 96 KiB of shared memory
+constexpr uint32_t kScanSmem = kScanChunk * 4u;  // dynamic shared memory of k_scan
+
+__device__ __forceinline__ void bulk_to_global(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+               "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// Chunk [c0, c0 + len) of the counts into s_cnt: the 16-byte-aligned part
+// by one bulk copy (thread 0) on `bar`, the rest by plain loads.  False when
+// the copy's wait runs out.
+__device__ __forceinline__ bool scan_stage(const KParams& p, uint32_t* s_cnt, uint64_t* bar, uint32_t c0,
+                                           uint32_t len, uint32_t& phase) {
+  const uint32_t bulk = len & ~3u;
+  if (bulk) {
+    if (threadIdx.x == 0) bulk_to_smem(s_cnt, p.cell_count + c0, bulk * 4u, bar);
+  }
+  if (threadIdx.x < len - bulk) s_cnt[bulk + threadIdx.x] = __ldcg(&p.cell_count[c0 + bulk + threadIdx.x]);
+  bool ok = true;
+  if (bulk) {
+    ok = mbar_wait(bar, phase);
+    if (!ok) mbar_wait(bar, phase);  // give the copy in flight more time to land before the CTA leaves
+    phase ^= 1u;
+  }
+  __syncthreads();
+  return ok;
+}
+
+__global__ void __launch_bounds__(1024) k_scan(KParams p) {
+  extern __shared__ __align__(128) uint32_t s_cnt[];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_stop, s_total, s_prefix, s_warp[32];
+  DevCtrl* c = p.ctrl;
+  if (threadIdx.x == 0) {
+    s_stop = ld_u32(&c->status) != 0u;
+    mbar_init(&s_bar);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  // the status is the previous kernels' and the same for every CTA: all
+  // return here together or none does
+  if (s_stop) return;
+  if (p.scan_withhold && blockIdx.x == 0) {  // test switch: CTA 0 never arrives
+    if (gridDim.x == 1 && threadIdx.x == 0) atomicOr(&c->status, kStatTimeout);
+    return;
+  }
+  // ranges of a multiple of 4 counts (16-byte aligned bulk copies)
+  const uint32_t per = ((p.n_cells + gridDim.x - 1u) / gridDim.x + 3u) & ~3u;
+  const uint32_t lo = min(blockIdx.x * per, p.n_cells), hi = min(lo + per, p.n_cells);
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t phase = 0;
+  bool ok = true;
+  // pass 1: the range's sum
+  uint32_t sum = 0;
+  for (uint32_t c0 = lo; c0 < hi && ok; c0 += kScanChunk) {
+    const uint32_t len = min(kScanChunk, hi - c0);
+    if (c0 != lo) __syncthreads();  // the previous chunk is summed
+    ok = scan_stage(p, s_cnt, &s_bar, c0, len, phase);
+    for (uint32_t i = threadIdx.x; i < len; i += 1024u) sum += s_cnt[i];
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(&c->status, kStatTimeout);
+    return;
+  }
+  sum = __reduce_add_sync(kFull, sum);
+  if (lane == 0) s_warp[warp] = sum;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t t = __reduce_add_sync(kFull, lane < (blockDim.x >> 5) ? s_warp[lane] : 0u);
+    if (lane == 0) p.tile_sums[blockIdx.x] = t;
+  }
+  if (!grid_barrier(c)) return;
+  // the counts before the range
+  if (warp == 0) {
+    uint32_t v = 0;
+    for (uint32_t b = lane; b < blockIdx.x; b += 32u) v += __ldcg(&p.tile_sums[b]);
+    v = __reduce_add_sync(kFull, v);
+    if (lane == 0) s_prefix = v;
+  }
+  __syncthreads();
+  // pass 2: each chunk scanned in shared memory, a run of q counts per thread
+  uint32_t carry = s_prefix;
+  const bool resident = hi - lo <= kScanChunk;  // the one chunk is still staged
+  for (uint32_t c0 = lo; c0 < hi; c0 += kScanChunk) {
+    const uint32_t len = min(kScanChunk, hi - c0);
+    if (!resident) {
+      __syncthreads();
+      if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // last chunk's store has read its source
+      __syncthreads();
+      if (!scan_stage(p, s_cnt, &s_bar, c0, len, phase)) {
+        if (threadIdx.x == 0) atomicOr(&c->status, kStatTimeout);
+        break;
+      }
+    }
+    const uint32_t q = (len + 1023u) >> 10;
+    const uint32_t b0 = min(threadIdx.x * q, len), b1 = min(b0 + q, len);
+    uint32_t s = 0;
+    for (uint32_t i = b0; i < b1; ++i) s += s_cnt[i];
+    uint32_t run = carry + block_exclusive_scan<1024>(s, &s_total);
+    carry += s_total;
+    for (uint32_t i = b0; i < b1; ++i) {
+      const uint32_t x = s_cnt[i];
+      s_cnt[i] = run;
+      run += x;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the writes above, seen by the bulk copy
+    __syncthreads();
+    const uint32_t bulk = len & ~3u;
+    if (threadIdx.x == 0 && bulk) bulk_to_global(p.cell_start + c0, s_cnt, bulk * 4u);
+    if (threadIdx.x < len - bulk) p.cell_start[c0 + bulk + threadIdx.x] = s_cnt[bulk + threadIdx.x];
+  }
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  if (blockIdx.x == gridDim.x - 1u && threadIdx.x == 0) {  // every count lies at or before its range's end
+    p.cell_start[p.n_cells] = carry;
+    c->n_sorted = carry;
+    if (carry > p.capacity) atomicOr(&c->status, kStatCapacity);
+  }
 }
 
 // Position of record r among the records of its cell [s, e) in canonical
@@ -1599,41 +1656,6 @@ __device__ __forceinline__ void commit_events(const KParams& p) {
   }
 }
 
-// Grid-wide barrier of a cooperative launch (every CTA resident): thread 0
-// of each CTA reads the generation, arrives on the counter, and either (the
-// last to arrive) resets the counter and advances the generation, or waits
-// for the generation to change.  The wait is bounded: after kGridSpins polls
-// the CTA raises kStatTimeout and the barrier returns false; the other CTAs
-// then run out at the same barrier or the next, so every CTA returns.
-constexpr uint32_t kGridSpins = 1u << 22;
-
-__device__ bool grid_barrier(DevCtrl* c) {
-  __shared__ uint32_t s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_ok = 1u;
-    const uint32_t gen = *(volatile uint32_t*)&c->bar_gen;
-    __threadfence();
-    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1u) {
-      atomicExch(&c->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
-    } else {
-      for (uint32_t spins = 0; *(volatile uint32_t*)&c->bar_gen == gen; ++spins) {
-        if (spins > kGridSpins) {
-          atomicOr(&c->status, kStatTimeout);
-          s_ok = 0u;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return s_ok != 0u;
-}
-
 // Candidate pairs above which the matching runs over the whole grid.
 constexpr uint32_t kMatchOneCta = 8192;
 
@@ -1861,7 +1883,6 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     __syncthreads();
   }
   commit_events(p);
-  for (uint32_t t = threadIdx.x; t < p.n_tiles; t += blockDim.x) p.scan_flags[t] = 0ull;
   for (uint32_t inst = threadIdx.x; inst < p.n_inst; inst += blockDim.x) {
     const DevInstance& I = p.inst[inst];
     advance_instance_step(p, inst, step_now);
@@ -1872,7 +1893,6 @@ __global__ void __launch_bounds__(1024) k_match(KParams p) {
     c->n_pairs = 0;
     c->n_big = 0;
     c->n_surf = 0;
-    c->scan_ticket = 0;
     c->surf_ticket = 0;
     c->deaths_last = s_deaths;
     c->n_slots = c->n_sorted;
@@ -2044,6 +2064,23 @@ void launch_match(const KParams& p, const LaunchShape& shape, cudaStream_t s) {
   else cudaLaunchKernelEx(&cfg, k_match<false>, p);
 }
 
+// The cell scan, cooperatively over at most shape.grid_scan CTAs (all
+// resident) and at most one per kScanTile cells.
+void launch_scan(const KParams& p, const LaunchShape& shape, cudaStream_t s) {
+  const uint32_t g = std::max(1u, std::min((uint32_t)std::max(shape.grid_scan, 1), p.n_tiles));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g);
+  cfg.blockDim = dim3(1024);
+  cfg.dynamicSmemBytes = kScanSmem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = g > 1 ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k_scan, p);
+}
+
 int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool has_uni, bool has_bim,
                  const LaunchShape& shape, cudaStream_t s, StageHook hook, void* ctx) {
   (void)has_uni;
@@ -2124,7 +2161,7 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
       BD_STREAM_LAUNCH(k_bin, 0);
       done("k_bin");
     }
-    k_scan<<<p.n_tiles, 1024, 0, s>>>(p);
+    launch_scan(p, shape, s);
     done("k_scan");
     BD_PAIRS_LAUNCH(true, kStagePairs);
     done("k_pairs_cells");
@@ -2140,7 +2177,7 @@ int enqueue_step(const KParams& p, Path path, bool table, bool has_zero, bool ha
   }
   BD_STREAM_LAUNCH_COMPACT(k_count);
   done("k_count");
-  k_scan<<<p.n_tiles, 1024, 0, s>>>(p);
+  launch_scan(p, shape, s);
   done("k_scan");
   BD_STREAM_LAUNCH_COMPACT(k_scatter);
   done("k_scatter");
@@ -2180,6 +2217,14 @@ int match_grid(int n_sm) {
   const int per_sm = a < b ? a : b;
   const int resident = per_sm > 0 ? per_sm * n_sm : 1;
   return resident < kMatchGrid ? resident : kMatchGrid;
+}
+
+int scan_grid(int n_sm) {
+  int a = 0;
+  if (cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanSmem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_scan, 1024, kScanSmem) != cudaSuccess || a < 1)
+    return 0;
+  return a * n_sm;
 }
 
 void enqueue_species_counts(const KParams& p, unsigned long long* counts, cudaStream_t s) {

@@ -30,9 +30,8 @@ struct KParams {
   uint32_t* zero_off;         // [I*Z + 1] prefix of zeroth-order births
   uint32_t* cell_count;       // [n_cells] particles per cell (returns to 0 each step)
   uint32_t* cell_start;       // [n_cells + 1] exclusive prefix of cell_count
-  uint32_t* tile_sums;        // [n_tiles] scan partials
-  unsigned long long* scan_flags; // [n_tiles] single-pass scan: state << 32 | sum, 0 between steps
-  uint32_t scan_withhold;     // test switch: tile 0 of the scan does not publish (its successors time out)
+  uint32_t* tile_sums;        // [n_tiles] the cell scan's per-CTA sums
+  uint32_t scan_withhold;     // test switch: CTA 0 of the cell scan never reaches its grid barrier
   uint32_t match_withhold;    // test switch: CTA 0 of the grid matcher never arrives (the others time out)
   DevPair* pairs;             // [pair_cap]
   unsigned long long* best;   // [capacity] matcher words, all ones between steps
@@ -71,11 +70,14 @@ struct LaunchShape {
   int grid_pairs, block_pairs;
   int min_blocks;             // register-capped streaming kernels: 1 (none), 4 (64 regs), 6 (40 regs)
   int grid_match;             // CTAs of the cooperative matcher (1 = one CTA, plain launch)
+  int grid_scan;              // most CTAs of the cooperative cell scan (all resident)
 };
 
 // CTAs of 1024 threads that the matcher can keep resident on n_sm SMs (the
 // size of its cooperative launch).
 int match_grid(int n_sm);
+// CTAs of 1024 threads that the cell scan can keep resident on n_sm SMs.
+int scan_grid(int n_sm);
 
 // Called after each kernel of a step is enqueued (stage name); lets the
 // profiler record an event between kernels.  nullptr = no callback.

@@ -111,11 +111,10 @@ struct DevCtrl {
   uint32_t bin_need;       // largest cell occupancy seen by a bin that overflowed
   uint32_t n_big;          // cells queued for the large-cell pair kernel
   uint32_t n_surf;         // records whose move meets a panel box (binned path with surfaces)
-  uint32_t scan_ticket;    // tiles taken by the single-pass cell scan of the step in flight
   uint32_t surf_ticket;    // queued records taken by k_bin_surface in the step in flight
-  // k_match over the whole grid (many candidate pairs): the grid barrier's
-  // arrival count and generation, the pending-pair counts of two rounds and
-  // the bimolecular deaths of the step
+  // the grid barrier (cell scan; k_match over the whole grid when a step
+  // has many candidate pairs): arrival count and generation; the matcher's
+  // pending-pair counts of two rounds and the bimolecular deaths of the step
   uint32_t bar_count, bar_gen;
   uint32_t match_next[2];
   uint32_t match_deaths;

@@ -250,10 +250,10 @@ BD_API bd_status bd_get_kernels_per_step(bd_handle h, int *n);
 BD_API bd_status bd_debug_get_slots(bd_handle h, float *xyz4, uint32_t *w, size_t cap, size_t *n);
 /* Cell start offsets of the last sorted step (ncells + 1 entries). */
 BD_API bd_status bd_debug_get_cells(bd_handle h, uint32_t *start, size_t cap, size_t *ncells);
-/* Test switch for the bounded wait of the single-pass cell scan: with on,
- * the scan's first tile keeps its sum to itself, so the next tile's wait
- * for it runs out (after about a second) and the step reports
- * BD_ERR_TIMEOUT instead of hanging.  No fault, trap or endless loop. */
+/* Test switch for the bounded waits of the cell scan's grid barrier: with
+ * on, CTA 0 of the scan never arrives at the barrier, so the other CTAs'
+ * waits run out (after about a second) and the step reports BD_ERR_TIMEOUT
+ * instead of hanging.  No fault, trap or endless loop. */
 BD_API bd_status bd_debug_withhold_scan(bd_handle h, int on);
 /* Test switch for the bounded waits of the matcher's grid barrier (steps
  * with more than 8,192 candidate pairs): with on, CTA 0 of the matcher

@@ -1,8 +1,8 @@
-"""The bounded waits on the device: the single-pass cell scan's look-back,
-and the grid barrier of the matcher on steps with many candidate pairs.
-With the test switch on, the scan's first tile keeps its sum to itself; the
-next tile's wait for it runs out, the step stops with BD_ERR_TIMEOUT, and the
-context stays usable (nothing faults, traps or hangs)."""
+"""The bounded waits on the device: the grid barriers of the cell scan and
+of the matcher on steps with many candidate pairs.  With a test switch on,
+CTA 0 of the kernel never arrives at its barrier; the other CTAs' waits run
+out, the step stops with BD_ERR_TIMEOUT, and the context stays usable
+(nothing faults, traps or hangs)."""
 import time
 
 import numpy as np
@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def system(seed):
-    # 40^3 cells: several scan tiles of 8,192 cells, so a tile has a predecessor
+    # 40^3 cells: several scan tiles of 8,192 cells, so the scan runs over several CTAs
     s = System((0, 0, 0), (20, 20, 20), dt=1e-3, seed=seed, normals="table", cell_size=0.5)
     A, B = s.add_species(1.0), s.add_species(1.0)
     s.add_reaction(2, [A, B], [A], 1.0)
