@@ -352,6 +352,25 @@ def test_sparse_clumps_bit_exact(sort):
     assert npairs > 100 and ev[0] > 0
 
 
+@pytest.mark.parametrize("sort", SORTS)
+def test_many_cells_scan_in_chunks_bit_exact(sort):
+    """9.3M cells: more than the cell scan's CTAs hold in shared memory at
+    once (two CTAs per SM, 24,576 counts each), so each CTA's range goes
+    through shared memory in several chunks, summed and then scanned again
+    chunk by chunk; the cell starts must equal the oracle's."""
+    side = 21.0
+    s = System((0, 0, 0), (side,) * 3, dt=1e-3, seed=43, normals="table", sort=sort, cell_size=0.1)
+    A, B, Cc = s.add_species(1.0), s.add_species(1.0), s.add_species(0.5)
+    s.add_reaction(2, [A, B], [Cc], 0.05)  # binding radius well below the 0.1 um cells
+    s.finalize()
+    n = 120_000
+    pos = uniform_positions(rng(43), n, (0, 0, 0), (side,) * 3)
+    s.set_particles(pos, (np.arange(n) % 2).astype(np.int32))
+    dims, _, _ = s.grid()
+    assert int(np.prod(dims.astype(np.int64))) > 2 * 160 * 24576
+    run_parity(s, 2)
+
+
 def test_steps_ordered_on_a_caller_stream():
     """bd_step_async on another stream gives the same trajectory as bd_step."""
     torch = pytest.importorskip("torch")
