@@ -1051,27 +1051,27 @@ __device__ __forceinline__ uint32_t forward_mask(const KParams& p, const Seeker&
   const float need = k.max_r + margin;
   const float fx = __fsub_rn(gx, (float)cx), fy = __fsub_rn(gy, (float)cy), fz = __fsub_rn(gz, (float)cz);
   const float hix = (1.0f - fx) * cl0, hiy = (1.0f - fy) * cl1, hiz = (1.0f - fz) * cl2;
-  // every forward neighbour lies across the +x, +y or +z face
-  const int zhi = (cz + 1 < (int)d2 && hiz <= need) ? 1 : 0;
-  const int yhi = (cy + 1 < (int)d1 && hiy <= need) ? 1 : 0;
-  const int xhi = (cx + 1 < (int)d0 && hix <= need) ? 1 : 0;
-  if ((zhi | yhi | xhi) == 0) return 0u;
+  // Every forward neighbour lies across the +x, +y or +z face.  Squared
+  // distance to the -/+ face along each axis, infinite where no
+  // cell lies beyond the face; a neighbour is marked when the sum over its
+  // axes, added as (x + y) + z, is within need^2.  No branch: the warp
+  // takes the records of a drain together, so every lane's marking used to
+  // run the loops of the slowest.
+  const float far = __int_as_float(0x7f800000);
   const float lox = fx * cl0, loy = fy * cl1;
   const float need2 = need * need;
-  const int ylo = (cy > 0 && loy <= need) ? -1 : 0;
-  const int xlo = (cx > 0 && lox <= need) ? -1 : 0;
-  uint32_t mask = 0;
-  for (int dz = 0; dz <= zhi; ++dz) {
-    const float ddz = dz > 0 ? hiz : 0.0f;
-    for (int dy = (dz > 0 ? ylo : 0); dy <= yhi; ++dy) {
-      const float ddy = dy < 0 ? loy : (dy > 0 ? hiy : 0.0f);
-      for (int dx = (dz > 0 || dy > 0 ? xlo : 1); dx <= xhi; ++dx) {
-        const float ddx = dx < 0 ? lox : (dx > 0 ? hix : 0.0f);
-        if (ddx * ddx + ddy * ddy + ddz * ddz > need2) continue;
-        const int b = dz > 0 ? 4 + (dy + 1) * 3 + (dx + 1) : (dy > 0 ? 2 + dx : 0);
-        mask |= 1u << b;
-      }
-    }
+  const float xm = cx > 0 ? lox * lox : far, xp = cx + 1 < (int)d0 ? hix * hix : far;
+  const float ym = cy > 0 ? loy * loy : far, yp = cy + 1 < (int)d1 ? hiy * hiy : far;
+  const float zp = cz + 1 < (int)d2 ? hiz * hiz : far;
+  uint32_t mask = xp <= need2 ? 1u : 0u;  // (+1, 0, 0)
+  mask |= (xm + yp <= need2 ? 1u : 0u) << 1;
+  mask |= (yp <= need2 ? 1u : 0u) << 2;
+  mask |= (xp + yp <= need2 ? 1u : 0u) << 3;
+  const float ey[3] = {ym, 0.0f, yp}, ex[3] = {xm, 0.0f, xp};
+#pragma unroll
+  for (int dy = 0; dy < 3; ++dy) {
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx) mask |= ((ex[dx] + ey[dy]) + zp <= need2 ? 1u : 0u) << (4 + dy * 3 + dx);
   }
   return mask;
 }
@@ -1098,15 +1098,20 @@ __device__ __forceinline__ void visit_cell(const KParams& p, DevCtrl* c, const S
   if (nn > kBigCell) return;  // pairs with large cells are found by k_pairs_big_pairs
   const CellView nb = cell_records<kBinned>(p, nkey, ns);
   // x words of the first members together (overlapping latencies); a full
-  // record only for members within the x window
+  // record only for members within the x window, taken from a bit mask
+  // (places past the cell read as all-ones bits, a NaN |dx|).  The mask in
+  // place of a branch per member: 0.248 against 0.261 ms on the 16M c3
+  // step, although only the records near a +face come here.
   constexpr uint32_t kBatch = 8;
   float xs[kBatch];
 #pragma unroll
-  for (uint32_t m = 0; m < kBatch; ++m) xs[m] = m < nn ? nb.ldg_x(m) : 0.0f;
+  for (uint32_t m = 0; m < kBatch; ++m) xs[m] = m < nn ? nb.ldg_x(m) : __uint_as_float(0xFFFFFFFFu);
+  uint32_t inx = 0;
 #pragma unroll
-  for (uint32_t m = 0; m < kBatch; ++m) {
-    if (m >= nn) break;
-    if (fabsf(__fsub_rn(xs[m], k.r.x)) > k.xlim) continue;
+  for (uint32_t m = 0; m < kBatch; ++m) inx |= (fabsf(__fsub_rn(xs[m], k.r.x)) <= k.xlim ? 1u : 0u) << m;
+  while (inx) {
+    const uint32_t m = (uint32_t)(__ffs(inx) - 1);
+    inx &= inx - 1u;
     const float4 q = nb.ldg(m);
     const int32_t b = pair_reaction(p, k, q);
     if (b >= 0) emit<kSingle>(p, c, k, ca, ns + canonical_rank(nb, 0, nn, m, q), b);
@@ -1337,19 +1342,22 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
       // on all four words.  cand: bit m = member m < 32 with |dx| in range
       // The first kRankBatch x words are loaded together, so their
       // latencies overlap (each group of kBinGroup members lies on its
-      // own line); larger cells continue one member at a time.
+      // own line); larger cells continue one member at a time.  The batch
+      // without a branch per member: 0.261 against 0.272 ms on the 16M c3
+      // step.
       constexpr uint32_t kRankBatch = 8;
       uint32_t rank = 0, le = 0, cand = 0;
       float xs[kRankBatch];
+      // (places past the cell read as all-ones bits: no rank, no le, and a
+      // NaN |dx| that is never in range, so the loop needs no branch)
 #pragma unroll
-      for (uint32_t m = 0; m < kRankBatch; ++m) xs[m] = m < on ? cb.ldg_x(m) : 0.0f;
+      for (uint32_t m = 0; m < kRankBatch; ++m) xs[m] = m < on ? cb.ldg_x(m) : __uint_as_float(0xFFFFFFFFu);
 #pragma unroll
       for (uint32_t m = 0; m < kRankBatch; ++m) {
-        if (m >= on) break;
         const uint32_t qb = __float_as_uint(xs[m]);
         rank += qb < rx ? 1u : 0u;
         le += qb <= rx ? 1u : 0u;
-        if (fabsf(__fsub_rn(xs[m], ra.x)) <= xlim) cand |= 1u << m;
+        cand |= (fabsf(__fsub_rn(xs[m], ra.x)) <= xlim ? 1u : 0u) << m;
       }
       for (uint32_t m = kRankBatch; m < on; ++m) {
         const float qx = cb.ldg_x(m);
