@@ -120,6 +120,7 @@ struct bd_system {
   DevBuf<DevUni> duni;
   DevBuf<DevBim> dbim;
   DevBuf<DevZero> dzero;
+  std::vector<DevZero> hzero;  // host copy of dzero
   DevBuf<double> dcdf;
   DevBuf<int32_t> dtable;
   DevBuf<float> dgauss;
@@ -195,6 +196,11 @@ KParams make_params(bd_system* h) {
   p.uni = h->duni.p;
   p.bim = h->dbim.p;
   p.zero = h->dzero.p;
+  if (!h->hinst.empty() && h->Z > 0 && h->Z <= 4) {
+    const size_t z0 = (size_t)h->hinst[0].block * h->Z;
+    for (int z = 0; z < h->Z; z++)
+      if (z0 + z < h->hzero.size()) p.zero0[z] = h->hzero[z0 + z];
+  }
   p.cdf = h->dcdf.p;
   p.bim_table = h->dtable.p;
   p.gauss = h->dgauss.p;
@@ -953,6 +959,7 @@ bd_status pack_blocks(bd_system* h) {
       cdf.insert(cdf.end(), P.cdf[r].begin(), P.cdf[r].end());
     }
   }
+  h->hzero = ze;
   if (h->host_only) return BD_OK;
   std::vector<float> gauss(4096);
   gauss_quantiles(gauss.data(), 4096);

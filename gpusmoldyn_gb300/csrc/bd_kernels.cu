@@ -344,11 +344,68 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 // ---------------------------------------------------------------- kernels
 
+// Fields of entry g (< 4) of KParams::zero0, read at fixed offsets.
+__device__ __forceinline__ void zero0_entry(const KParams& p, uint32_t g, uint32_t& off, uint32_t& len,
+                                            int32_t& kmin, uint32_t& rxn) {
+  off = p.zero0[0].cdf_off, len = p.zero0[0].cdf_len, kmin = p.zero0[0].kmin, rxn = p.zero0[0].rxn;
+#pragma unroll
+  for (uint32_t z = 1; z < 4; ++z)
+    if (g == z) off = p.zero0[z].cdf_off, len = p.zero0[z].cdf_len, kmin = p.zero0[z].kmin, rxn = p.zero0[z].rxn;
+}
+
 __global__ void __launch_bounds__(1024) k_zeroth(KParams p, int check_append) {
   __shared__ uint32_t s_total;
   DevCtrl* c = p.ctrl;
-  if (ld_u32(&c->status)) return;
   const uint32_t nz = p.n_inst * p.Z;
+  if (p.n_inst == 1 && nz <= 4u) {
+    // One instance, at most four reactions: the entries come from the
+    // kernel parameters and the status, step and flags are loaded
+    // together, so the counts wait on one round of global loads (the
+    // CDFs) instead of a chain of four.  Counting as below.
+    __shared__ uint32_t s_part[32], s_cnt[4];
+    const uint32_t status = ld_u32(&c->status), step = p.inst_step[0];
+    const bool adv = advancing(p.inst_flags[0]);
+    const uint32_t G = nz > 2u ? 256u : (nz > 1u ? 512u : 1024u);  // threads per entry
+    const uint32_t g = threadIdx.x / G, t = threadIdx.x % G;
+    uint32_t off, len, rxn;
+    int32_t kmin;
+    uint32_t le = 0;
+    if (g < nz && adv) {
+      zero0_entry(p, g, off, len, kmin, rxn);
+      const U4 r = philox(U4{g, step, kTagZeroCount, 0u}, p.inst0.key_lo, p.inst0.key_hi);
+      const double u = u53_to_unit(r.x, r.y);
+      const double* cdf = p.cdf + off;
+      for (uint32_t k = t; k < len; k += G) le += cdf[k] <= u ? 1u : 0u;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) le += __shfl_xor_sync(kFull, le, d);
+    if ((threadIdx.x & 31u) == 0) s_part[threadIdx.x >> 5] = le;
+    __syncthreads();
+    if (threadIdx.x < nz) {
+      uint32_t cnt = 0;
+      if (adv) {
+        zero0_entry(p, threadIdx.x, off, len, kmin, rxn);
+        uint32_t below = 0;
+        for (uint32_t w = 0; w < G / 32u; ++w) below += s_part[threadIdx.x * (G / 32u) + w];
+        cnt = (uint32_t)kmin + min(below, len - 1u);
+        if (cnt && !status) atomicAdd(&p.pending[rxn], (unsigned long long)cnt);
+      }
+      s_cnt[threadIdx.x] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !status) {
+      uint32_t carry = 0;
+      for (uint32_t e = 0; e < nz; ++e) {
+        p.zero_off[e] = carry;
+        carry += s_cnt[e];
+      }
+      p.zero_off[nz] = carry;
+      c->n_virtual = carry;
+      if (check_append && (uint64_t)c->n_slots + carry > p.capacity) atomicOr(&c->status, kStatCapacity);
+    }
+    return;
+  }
+  if (ld_u32(&c->status)) return;
   if (nz <= 32u) {
     // Few entries (one instance, a few reactions): a group of at least 32
     // threads per entry counts the CDF values at or below u.  The CDF does

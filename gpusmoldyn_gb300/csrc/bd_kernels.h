@@ -28,6 +28,7 @@ struct KParams {
   uint32_t* inst_frozen;      // [I] global step (low 32 bits) at which an instance froze
   uint32_t* inst_slot_base;   // [I] first slot of each instance in the current state
   uint32_t* zero_off;         // [I*Z + 1] prefix of zeroth-order births
+  DevZero zero0[4];           // instance 0's zeroth-order entries when Z <= 4 (k_zeroth's one-instance path)
   uint32_t* cell_count;       // [n_cells] particles per cell (returns to 0 each step)
   uint32_t* cell_start;       // [n_cells + 1] exclusive prefix of cell_count
   uint32_t* tile_sums;        // [n_tiles] the cell scan's per-CTA sums
