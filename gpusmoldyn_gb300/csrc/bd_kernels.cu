@@ -1211,9 +1211,10 @@ __device__ __forceinline__ void visit_cell(const KParams& p, DevCtrl* c, const S
 // next step; otherwise from the compact scatter buffer.
 //
 // Binned path: bulk-copy staging of each task's first bin group (kStage).
-// Measured slower on the 16M c3 step (0.360 against 0.338 ms): four CTAs'
-// staging buffers take the L1 space that the neighbour visits hit in.  Kept
-// selectable.
+// Measured slower on the 16M c3 step (0.325 against 0.272 ms with the
+// record stream; 0.360 against 0.338 ms before it): four CTAs' staging
+// buffers take the L1 space that the rank loads and neighbour visits hit
+// in.  Kept selectable; the parity tests pass with it.
 constexpr bool kStagePairs = false;
 
 constexpr uint32_t kFaceQueue = 64;  // queued records per warp (< 32 between drains, + one round's push)
