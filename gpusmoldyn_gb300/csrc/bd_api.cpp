@@ -404,6 +404,7 @@ bd_status create_common(const bd_config* cfg, const bd_instance_desc* inst, int 
   h->shape.grid_pairs = h->n_sm * 4;
   h->shape.grid_match = h->host_only ? 1 : match_grid(h->n_sm);
   h->shape.grid_scan = h->host_only ? 1 : scan_grid(h->n_sm);
+  h->shape.grid_big = h->host_only ? 1 : big_grid(h->n_sm);
   memset(h->hctrl, 0, sizeof(DevCtrl));
   cudaMemset(h->ctrl.p, 0, sizeof(DevCtrl));
   *out = h;

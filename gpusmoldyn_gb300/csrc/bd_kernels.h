@@ -72,6 +72,7 @@ struct LaunchShape {
   int min_blocks;             // register-capped streaming kernels: 1 (none), 4 (64 regs), 6 (40 regs)
   int grid_match;             // CTAs of the cooperative matcher (1 = one CTA, plain launch)
   int grid_scan;              // most CTAs of the cooperative cell scan (all resident)
+  int grid_big;               // CTAs of the large-cell kernel (all resident)
 };
 
 // CTAs of 1024 threads that the matcher can keep resident on n_sm SMs (the
@@ -79,6 +80,8 @@ struct LaunchShape {
 int match_grid(int n_sm);
 // CTAs of 1024 threads that the cell scan can keep resident on n_sm SMs.
 int scan_grid(int n_sm);
+// CTAs of the large-cell kernel: at most 304, all resident on n_sm SMs.
+int big_grid(int n_sm);
 
 // Called after each kernel of a step is enqueued (stage name); lets the
 // profiler record an event between kernels.  nullptr = no callback.

@@ -404,3 +404,33 @@ def test_competing_reactions_bit_exact(sort):
     s.set_particles(pos, (np.arange(6000) % 2).astype(np.int32))
     _, npairs, ev = run_parity(s, 15)
     assert ev[0] > 30 and ev[1] > 10 and ev[2] > 60
+
+
+def test_handles_step_concurrently_as_alone():
+    """Two handles stepping at the same time on their own streams, each
+    with cooperative launches that fill the GPU (the cell scan over every
+    SM, the matcher's grid on a dense system), give the results each gives
+    alone: the launches of one handle never wait on CTAs of the other."""
+    from gpusmoldyn_gb300 import configs
+
+    def big(seed):
+        side = 200.0 * (8_000_000 / 16_000_000) ** (1 / 3)
+        return configs.build_c3(n=8_000_000, side=side, seed=seed, normals="table")
+
+    def dense(seed):
+        return dense_a_b(2000, 2000, 2.0, seed=seed, kon=5.0)
+
+    alone = []
+    for make, seed in ((big, 51), (dense, 52)):
+        s = make(seed)
+        s.step(20)
+        s.synchronize()
+        alone.append(gpu_records(s))
+        s.close()
+    a, b = big(51), dense(52)
+    a.step(20)
+    b.step(20)
+    a.synchronize()
+    b.synchronize()
+    np.testing.assert_array_equal(gpu_records(a), alone[0])
+    np.testing.assert_array_equal(gpu_records(b), alone[1])
