@@ -1286,10 +1286,20 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
   __shared__ uint2 s_meta[8][kCellRing];
   __shared__ FaceQueue s_face[kHasBim ? 8 : 1];
   __shared__ float s_maxr[kSingle ? kCtxSpecies : 1];
+  // one-instance kernels: per species, the near-face thresholds of
+  // near_forward_face in grid units (x, y, z), computed once per CTA with
+  // the same operations (0.2412 -> 0.2403 ms on the 16M c3 step)
+  __shared__ float4 s_near[kSingle ? kCtxSpecies : 1];
   __shared__ __align__(128) float4 s_stage[kStage ? 8 : 1][kStage ? 2 : 1][kStage ? 32 * kBinGroup : 1];
   __shared__ uint64_t s_bar[kStage ? 8 : 1][2];
   if (kSingle) {  // before any warp may leave: one barrier for the whole CTA
-    for (uint32_t t = threadIdx.x; t < p.S; t += blockDim.x) s_maxr[t] = p.species[p.inst0.block * p.S + t].max_r;
+    for (uint32_t t = threadIdx.x; t < p.S; t += blockDim.x) {
+      const float mr = p.species[p.inst0.block * p.S + t].max_r;
+      s_maxr[t] = mr;
+      const DevInstance& I = p.inst0;
+      const float slack = 1.01f * (mr + p.prune_margin * fminf(I.cell[0], fminf(I.cell[1], I.cell[2])));
+      s_near[t] = make_float4(slack * I.inv[0], slack * I.inv[1], slack * I.inv[2], 0.0f);
+    }
     __syncthreads();
   }
   const bool adv0 = kSingle ? advancing(ld_u32(&p.inst_flags[0])) : true;
@@ -1458,7 +1468,16 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
           const int32_t bb = pair_reaction(p, k, qm);
           if (bb >= 0) emit<kSingle>(p, c, k, ca, ocs + canonical_rank(cb, 0, on, m, qm), bb);
         }
-        near = near_forward_face<kSingle>(p, k);
+        if (kSingle) {
+          const float4 sn = s_near[rec_w(ra) & kSpeciesMask];
+          const DevInstance& I = p.inst0;
+          const float gx = __fmul_rn(__fsub_rn(ra.x, I.lo[0]), I.inv[0]);
+          const float gy = __fmul_rn(__fsub_rn(ra.y, I.lo[1]), I.inv[1]);
+          const float gz = __fmul_rn(__fsub_rn(ra.z, I.lo[2]), I.inv[2]);
+          near = !(1.0f - (gx - floorf(gx)) > sn.x && 1.0f - (gy - floorf(gy)) > sn.y && 1.0f - (gz - floorf(gz)) > sn.z);
+        } else {
+          near = near_forward_face<kSingle>(p, k);
+        }
       }
     }
     if (kHasBim) {
