@@ -881,8 +881,8 @@ __device__ __forceinline__ bool scan_stage(const KParams& p, uint32_t* s_cnt, ui
     if (!ok) mbar_wait(bar, phase);  // give the copy in flight more time to land before the CTA leaves
     phase ^= 1u;
   }
-  __syncthreads();
-  return ok;
+  // one answer for the whole CTA, so that its threads leave or go on together
+  return __syncthreads_and(ok) != 0;
 }
 
 __global__ void __launch_bounds__(1024) k_scan(KParams p) {
@@ -1389,7 +1389,8 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
       loaded += __shfl_sync(kFull, incl, 31);
       if (sl) o1 = n > 0 ? off : ~0u;
       else o0 = n > 0 ? off : ~0u;
-      if (kStage && !mbar_wait(&s_bar[warp][sl], (opened >> 1) & 1u)) {
+      // (one answer for the warp: its lanes leave or go on together)
+      if (kStage && !__all_sync(kFull, mbar_wait(&s_bar[warp][sl], (opened >> 1) & 1u))) {
         // give up: record the timeout and let the copies still in flight land
         if (lane == 0) atomicOr(&c->status, kStatTimeout);
         for (uint32_t i = opened; i < staged; ++i) mbar_wait(&s_bar[warp][i & 1u], (i >> 1) & 1u);
