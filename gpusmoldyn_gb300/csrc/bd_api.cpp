@@ -1928,7 +1928,10 @@ BD_API const char* bd_stage_name(bd_handle h, int k) {
 BD_API bd_status bd_get_kernels_per_step(bd_handle h, int* n) {
   if (!h || !n) return BD_ERR_INVALID_ARGUMENT;
   if (h->diffuse_only()) *n = (h->Z > 0 ? 2 : 0) + 2;
-  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 5 : 6) + (h->B > 0 ? 1 : 0) + (h->binned && !h->panels.empty() ? 1 : 0);
+  // binned: k_bin, k_scan, k_pairs_cells, k_pairs_big, k_match (+ k_bin_surface
+  // with panels); compact: k_count, k_scan, k_scatter, k_pairs_cells,
+  // k_pairs_big, k_match; k_zeroth first with zeroth-order reactions
+  else *n = (h->Z > 0 ? 1 : 0) + (h->binned ? 5 : 6) + (h->binned && !h->panels.empty() ? 1 : 0);
   return BD_OK;
 }
 
