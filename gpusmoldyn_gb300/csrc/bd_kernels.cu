@@ -765,9 +765,6 @@ struct CellView {
   __device__ __forceinline__ float ldg_x(uint32_t m) const {
     return __ldg(reinterpret_cast<const float*>(base + at(m)));
   }
-  __device__ __forceinline__ float ldg_y(uint32_t m) const {
-    return __ldg(reinterpret_cast<const float*>(base + at(m)) + 1);
-  }
   __device__ __forceinline__ float2 ldg_xy(uint32_t m) const {
     return __ldg(reinterpret_cast<const float2*>(base + at(m)));
   }
@@ -790,10 +787,6 @@ struct BinView {
   __device__ __forceinline__ float ldg_x(uint32_t m) const {
     if (kStage && m < kBinGroup) return sm[m].x;
     return g.ldg_x(m);
-  }
-  __device__ __forceinline__ float ldg_y(uint32_t m) const {
-    if (kStage && m < kBinGroup) return sm[m].y;
-    return g.ldg_y(m);
   }
   __device__ __forceinline__ float2 ldg_xy(uint32_t m) const {
     if (kStage && m < kBinGroup) return make_float2(sm[m].x, sm[m].y);
