@@ -642,7 +642,7 @@ bd_status upload_particles(bd_system* h, const float* xyz4, const int* species, 
     BD_CUDA(cudaMemcpyAsync(d_start, start.data(), (I + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
     BD_CUDA(cudaMemcpyAsync(d_boxes, boxes.data(), boxes.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     BD_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(uint32_t), h->stream));
-    up = UploadArgs{d_xyz4, d_species, d_start, d_boxes, n, I, h->S, d_bad};
+    up = UploadArgs{d_xyz4, d_species, d_start, d_boxes, n, I, h->S, d_bad, 0u};
     enqueue_upload_check(up, h->stream);
     BD_CUDA(cudaGetLastError());
     uint32_t bad = 0;
@@ -1038,7 +1038,7 @@ BD_API bd_status bd_finalize(bd_handle h) {
   h->U = (int)h->uni_list.size();
   h->B = (int)h->bim_list.size();
   h->Z = (int)h->zero_list.size();
-  const int S = h->S, U = h->U, B = h->B, Z = h->Z;
+  const int S = h->S, B = h->B;
 
   // pair table: the last reaction listed for a pair wins (particleSystem.cpp:656-669),
   // or, with competing reactions, the first of the pair's chain; a reaction
