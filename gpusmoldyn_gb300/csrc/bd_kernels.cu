@@ -1427,16 +1427,23 @@ __global__ void __launch_bounds__(256, 4) k_pairs_cells(KParams p) {
       // never in range.
       constexpr uint32_t kRankBatch = 8;
       uint32_t rank = 0, le = 0, cand = 0;
+      // members [0, 6) always, [6, 8) only when a lane of the warp has more
+      // than six (0.2386 -> 0.2378 ms on the 16M c3 step)
+      constexpr uint32_t kRankFirst = 6;
       float2 xs[kRankBatch];
+      auto rank_members = [&](uint32_t m0, uint32_t m1) {
 #pragma unroll
-      for (uint32_t m = 0; m < kRankBatch; ++m) xs[m] = m < on ? cb.ldg_xy(m) : make_float2(__uint_as_float(0xFFFFFFFFu), 0.0f);
+        for (uint32_t m = m0; m < m1; ++m) xs[m] = m < on ? cb.ldg_xy(m) : make_float2(__uint_as_float(0xFFFFFFFFu), 0.0f);
 #pragma unroll
-      for (uint32_t m = 0; m < kRankBatch; ++m) {
-        const uint32_t qb = __float_as_uint(xs[m].x);
-        rank += qb < rx ? 1u : 0u;
-        le += qb <= rx ? 1u : 0u;
-        cand |= (fabsf(__fsub_rn(xs[m].x, ra.x)) <= xlim && fabsf(__fsub_rn(xs[m].y, ra.y)) <= xlim ? 1u : 0u) << m;
-      }
+        for (uint32_t m = m0; m < m1; ++m) {
+          const uint32_t qb = __float_as_uint(xs[m].x);
+          rank += qb < rx ? 1u : 0u;
+          le += qb <= rx ? 1u : 0u;
+          cand |= (fabsf(__fsub_rn(xs[m].x, ra.x)) <= xlim && fabsf(__fsub_rn(xs[m].y, ra.y)) <= xlim ? 1u : 0u) << m;
+        }
+      };
+      rank_members(0, kRankFirst);
+      if (__any_sync(__activemask(), on > kRankFirst)) rank_members(kRankFirst, kRankBatch);
       for (uint32_t m = kRankBatch; m < on; ++m) {
         const float qx = cb.ldg_x(m);
         const uint32_t qb = __float_as_uint(qx);
