@@ -1738,9 +1738,10 @@ __device__ void big_pairs(const KParams& p, DevCtrl* c, uint32_t nbig) {
 // by every CTA, in one launch (cooperative when there are pairs to find,
 // so that the barrier waits only on resident CTAs).  Every CTA reads the
 // same final count of queued cells, so when none is large they all leave
-// at once: one empty launch per step instead of two, 3.3 us less on the
-// 16M c3 step.  The first step that queues a cell without big_scratch in
-// place raises kStatScratch; the host allocates it and replays the step.
+// at once: one empty launch per step instead of two (the two empty
+// launches cost 3.3 us per 16M c3 step; the one measured within noise of
+// them).  The first step that queues a cell without big_scratch in place
+// raises kStatScratch; the host allocates it and replays the step.
 template <bool kHasBim, bool kBinned>
 __global__ void __launch_bounds__(256) k_pairs_big(KParams p) {
   __shared__ float4 s_rec[kBigChunk];
